@@ -1,0 +1,393 @@
+"""Benchmark of the GB300 RTM engine on the large plain 2D acoustic RTM workload.
+
+Workload (one "step" = one RTM shot: forward modelling with illumination +
+backward propagation with zero-lag imaging): grid 1000 x 4000, dx = dz = 2.5 m,
+6 Hz Ricker, dt = 0.25 ms, nt = 8000, 4000 surface receivers, source on row 2;
+seeded synthetic layered-gradient model with three faults, migration model
+Gaussian-smoothed.  Metric: RTM Gpts/s, counting 2 * nz * nx * nt point-updates
+per shot (forward + backward; recomputation not counted).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* ``value``: device-timed (CUDA events on the engine stream), shot inputs already
+  resident in HBM (``w2d_migrate_staged``), images stacked on the device.
+* ``e2e``: the public drop-in call ``TSWRTMEngine.migrate_shot`` with host arrays
+  in page-locked memory; the host->device copies of the gather, wavelet and both
+  velocity models and the device->host copies of image and illumination are
+  inside the timed region.
+* ``roofline``: the fused step kernel, algorithmic bytes of all step launches in
+  the timed region over the device time of the region, against the measured HBM
+  copy bandwidth.
+* ``cpu_baseline``: the reference's CPU path (wave2d.c + its Python time loops,
+  restated in oracle/) timed on this host's cores over a bounded sample.
+* ``--impl reference``: that CPU implementation alone, each step a bounded sample
+  of the same workload (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "RTM Gpts/s"
+UNIT = "Gpts/s"
+L2_NOTE = ("inputs larger than L2: every shot streams a 128 MB gather and a 64 GB forward "
+           "snapshot store through HBM")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier / max-reduce over ranks (torch.distributed only when WORLD_SIZE > 1)."""
+
+    def __init__(self, backend):
+        self.rank, self.world, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        dev = "cuda" if self.td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, or None."""
+    p = os.path.join(REPO, "profiles", "acoustic_step_large_plain.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str, rank: int):
+        self.proc = None
+        self.gpu = gpu_id
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_rank{rank}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+                except ValueError:
+                    continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        loaded = [r[0] for r in rows if r[2] > 200.0] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# ------------------------------------------------------------------------------ workload
+
+def make_survey(nt):
+    from das_gb300.synthetic import plain_large
+    return plain_large(seed=0, nt=nt)
+
+
+def bytes_per_shot(sv, interval):
+    """Algorithmic HBM bytes of the fused step launches of one RTM shot.
+
+    Forward step: read p_curr, p_prev, vel^2 dt^2, write p_next = 16 B/pt; on
+    snapshot steps +4 (snapshot store) +8 (illumination read-modify-write).
+    Backward step: 16 B/pt; on imaging steps +4 (snapshot read) +8 (image RMW).
+    """
+    P = sv.nz * sv.nx
+    n_snaps = (sv.nt - 1) // interval + 1
+    return 2 * sv.nt * P * 16 + n_snaps * P * 12 * 2
+
+
+def cpu_sample(sv, gather, nt_sample, threads):
+    """Reference CPU path (oracle restatement of wave2d.c + its Python loops) on a sample."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as o
+    kind = "reference" if o.reference_available() else "port"
+    o.set_backend("reference" if kind == "reference" else "native")
+    g = o.Grid(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
+    sponge = g.sponge()
+    w = sv.wavelet[:nt_sample]
+    data = np.ascontiguousarray(gather[:nt_sample])
+    t0 = time.perf_counter()
+    o.migrate_shot(g, sv.vel_mig, sv.vel_mig, w, int(sv.src_ix[0]), sv.src_iz, data, sv.rec_ix,
+                   sv.rec_iz, 2, sponge=sponge, native=True)
+    el = time.perf_counter() - t0
+    pts = 2 * sv.nz * sv.nx * nt_sample
+    return pts / el / 1e9, el, kind
+
+
+def run_reference(args, dist):
+    """--impl reference: the CPU implementation timed on the host cores (rank 0 only)."""
+    if dist.rank != 0:
+        return
+    threads = len(os.sched_getaffinity(0))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from das_gb300.synthetic import plain_large
+    nt_sample = args.cpu_nt
+    sv = plain_large(seed=0, nt=8000)
+    rng = np.random.default_rng(1)
+    gather = (rng.standard_normal((nt_sample, sv.nx)) * 1e-9).astype(np.float32)
+    vals = []
+    kind = None
+    for k in range(args.warmup + args.steps):
+        v, el, kind = cpu_sample(sv, gather, nt_sample, threads)
+        if k >= args.warmup:
+            vals.append((v, el))
+    gpts = sum(2 * sv.nz * sv.nx * nt_sample for _ in vals) / sum(e for _, e in vals) / 1e9
+    ms = 1e3 * sum(e for _, e in vals) / len(vals)
+    sample = (f"migrate_shot on the 1000x4000 grid truncated to nt={nt_sample} steps "
+              f"(forward+backward, snapshot interval 2, 4000 receivers) per step")
+    out = {"impl": "reference", "metric": METRIC, "value": gpts, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": sv.name, "nz": sv.nz, "nx": sv.nx, "nt": sv.nt,
+                      "sampled_nt": nt_sample, "parallelism": "cpu"},
+           "cpu_baseline": {"value": gpts, "unit": UNIT, "cores": threads, "kind": kind,
+                            "sample": sample},
+           "e2e": {"value": gpts, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, dist):
+    import das_gb300
+    from das_gb300 import _lib
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D
+    from das_gb300.pinned import pinned_array
+
+    lib = das_gb300.lib()
+    if dist.world > 1:
+        _lib.check(lib.w2d_set_device(dist.local))
+    bus = ctypes.create_string_buffer(64)
+    gpu_id = bus.value.decode() if lib.w2d_device_pci_bus_id(bus, 64) == 0 else str(dist.local)
+    sv = make_survey(args.nt)
+    interval = 2
+    solver = WaveSolver2D(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
+    if args.tile:
+        solver.tile = tuple(int(t) for t in args.tile.split(","))
+    eng = solver._eng()
+    K, W = args.steps, args.warmup
+    n_sh = K + W
+    # this rank's shots (weak scaling: every rank migrates its own K + W shots)
+    shots = [int(sv.src_ix[(dist.rank * n_sh + k) * 7 % len(sv.src_ix)]) for k in range(n_sh)]
+
+    # observed gathers: forward modelling in the true model on the GPU (untimed set-up)
+    gathers = []
+    for six in shots[: min(n_sh, args.distinct_gathers)]:
+        rec, _ = solver.forward_propagate_acoustic(sv.vel_true, sv.wavelet, six, sv.src_iz,
+                                                   sv.rec_ix, sv.rec_iz)
+        gathers.append(rec)
+    gathers = [gathers[k % len(gathers)] for k in range(n_sh)]
+    rix = sv.rec_ix.astype(np.int32)
+    fm = FloodModels(sv.vel_true, sv.vel_mig, sv.vel_mig, 0, 0)
+    solver._set_velocity(0, sv.vel_mig)
+    solver._set_velocity(1, sv.vel_mig)
+    for k in range(n_sh):
+        _lib.check(lib.w2d_shot_stage(eng, k, sv.wavelet.ctypes.data, sv.nt,
+                                      gathers[k].ctypes.data, sv.nx))
+    _lib.check(lib.w2d_stack_reset(eng))
+    storage = {"auto": 0, "all": 1, "checkpoint": 2}[args.storage]
+
+    def staged(k):
+        _lib.check(lib.w2d_migrate_staged(eng, k, shots[k], sv.src_iz, rix.ctypes.data, sv.nx,
+                                          sv.rec_iz, interval, storage, None, None))
+        return solver.last_stats()
+
+    for k in range(W):
+        staged(k)
+    clocks = Clocks(gpu_id, dist.rank)
+    clocks.start()
+    dist.barrier()
+    _lib.check(lib.w2d_engine_timer_start(eng))
+    launches = 0
+    recompute = 0
+    used = None
+    t_wall = time.perf_counter()
+    for k in range(W, W + K):
+        st = staged(k)
+        launches += st["step_launches"]
+        recompute += st["recomputed_steps"]
+        used = st["storage"]
+    ms = ctypes.c_float()
+    _lib.check(lib.w2d_engine_timer_stop(eng, ctypes.byref(ms)))
+    wall = time.perf_counter() - t_wall
+    dist.barrier()
+    clk = clocks.stop()
+    dev_s = dist.max(ms.value / 1e3)
+    pts = sv.counted_points_per_shot()
+    value = pts * K * dist.world / dev_s / 1e9
+
+    # roofline of the fused step kernel over the timed region
+    peak, peak_kind = measured_peaks()
+    step_launches_per_shot = 2 * sv.nt + recompute // max(K, 1)
+    algo_bytes = bytes_per_shot(sv, interval) * K + recompute * sv.nz * sv.nx * 16
+    achieved = algo_bytes / (ms.value / 1e3) / 1e9
+    per_launch = algo_bytes / (step_launches_per_shot * K)
+    traffic = committed_traffic()
+
+    # end-to-end through the public drop-in call, inputs in page-locked host memory
+    ke = max(1, min(K, args.e2e_steps))
+    pin_g = [pinned_array(gathers[W + k].shape) for k in range(ke)]
+    for k in range(ke):
+        pin_g[k][...] = gathers[W + k]
+    pin_w = pinned_array(sv.wavelet.shape)
+    pin_w[...] = sv.wavelet
+    pin_vs = pinned_array(sv.vel_mig.shape)
+    pin_vs[...] = sv.vel_mig
+    pin_vr = pinned_array(sv.vel_mig.shape)
+    pin_vr[...] = sv.vel_mig
+    fm_p = FloodModels(sv.vel_true, pin_vs, pin_vr, 0, 0)
+    eng_api = TSWRTMEngine(solver, storage=args.storage)
+    eng_api.migrate_shot(fm_p, pin_w, shots[0], sv.src_iz, pin_g[0], sv.rec_ix, sv.rec_iz, interval)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(ke):
+        img, ill = eng_api.migrate_shot(fm_p, pin_w, shots[W + k], sv.src_iz, pin_g[k], sv.rec_ix,
+                                        sv.rec_iz, interval)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = pts * ke * dist.world / e2e_s / 1e9
+    h2d = gathers[0].nbytes + sv.wavelet.nbytes + 2 * sv.vel_mig.nbytes + rix.nbytes
+    d2h = 2 * sv.nz * sv.nx * 4
+
+    cpu = None
+    if dist.rank == 0 and args.cpu_nt > 0:
+        threads = len(os.sched_getaffinity(0))
+        v, el, kind = cpu_sample(sv, gathers[0], args.cpu_nt, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"migrate_shot on the 1000x4000 grid truncated to nt={args.cpu_nt} "
+                         f"(forward+backward, interval 2, 4000 receivers), {el:.1f} s"}
+
+    if dist.rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": K,
+               "warmup": W, "ms_per_step": dev_s * 1e3 / K, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded layered-gradient model with 3 faults; gathers "
+                       "forward-modelled on the GPU in the true model)",
+               "config": {"workload": sv.name, "nz": sv.nz, "nx": sv.nx, "nt": sv.nt,
+                          "dx": sv.dx, "dt": sv.dt, "receivers": int(len(sv.rec_ix)),
+                          "shots_per_step": 1, "snapshot_interval": interval,
+                          "storage": used, "tile": list(solver.tile or (8, 4)),
+                          "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
+               "shots_per_s": K * dist.world / dev_s,
+               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": traffic,
+                            "peak_source": f"{peak_kind} hbm_gbs",
+                            "kernel": "acoustic_step_kernel (fused forward / backward+imaging)",
+                            "algorithmic_bytes_per_launch": per_launch},
+               "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                       "d2h_bytes_per_step": int(d2h), "steps": ke,
+                       "api": "TSWRTMEngine.migrate_shot (pinned host arrays)"},
+               "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+               "wall_s_timed_region": wall}
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nt", type=int, default=8000)
+    ap.add_argument("--storage", default="auto", choices=["auto", "all", "checkpoint"])
+    ap.add_argument("--tile", default="")
+    ap.add_argument("--cpu-nt", type=int, default=60)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--distinct-gathers", type=int, default=2)
+    args = ap.parse_args()
+    os.environ.setdefault("OMP_NUM_THREADS", str(len(os.sched_getaffinity(0))))
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        dist = Dist("gloo")
+        try:
+            run_reference(args, dist)
+        finally:
+            dist.close()
+        return
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+    dist = Dist("nccl" if world > 1 else "gloo")
+    try:
+        run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1059 @@
+// engine.cu -- whole-loop acoustic engine: device-resident wavefields, fused
+// step launches for forward modelling, backward propagation with imaging, and
+// forward+backward migration of a shot with full snapshot storage or
+// checkpointed recomputation.  Also the reference-compatible per-step
+// acoustic_2d_step / correlate_imaging_condition entry points.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "acoustic_kernels.cuh"
+#include "w2d_common.cuh"
+#include "wave2d_cuda.h"
+
+namespace w2d {
+
+float cerjan_value(int d, float alpha);
+
+// ---- small elementwise kernels ------------------------------------------------
+__global__ void v2dt2_kernel(float* out, const float* vel, size_t n, float dt2)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float v = vel[i];
+        out[i] = fmul(fmul(v, v), dt2);  // v * v * dt2 (wave2d.c:60-61)
+    }
+}
+
+__global__ void scale_kernel(float* a, size_t n, float s)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        a[i] = fmul(a[i], s);
+}
+
+__global__ void add_kernel(float* acc, const float* x, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        acc[i] = fadd(acc[i], x[i]);
+}
+
+__global__ void correlate_kernel(const float* src, const float* rec, float* image, size_t n,
+                                 float dt)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        image[i] = fadd(image[i], fmul(fmul(src[i], rec[i]), dt));
+}
+
+static int grid_for(size_t n, int block = 256)
+{
+    size_t b = (n + block - 1) / block;
+    return (int)std::min<size_t>(b, 152 * 16);
+}
+
+// ---- tile-shape dispatch ------------------------------------------------------
+struct TileShape {
+    int warps, rpw;
+    int tz() const { return warps * rpw; }
+};
+
+static bool tile_supported(int warps, int rpw)
+{
+    return (warps == 8 && rpw == 4) || (warps == 4 && rpw == 8) || (warps == 8 && rpw == 8) ||
+           (warps == 4 && rpw == 4) || (warps == 16 && rpw == 4);
+}
+
+template <int W, int R>
+static void launch_t(const CUtensorMap& tm, const AcGeom& g, const AcStep& s, cudaStream_t st)
+{
+    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + W * R - 1) / (W * R));
+    acoustic_step_kernel<W, R><<<grid, W * 32, 0, st>>>(tm, g, s);
+}
+
+static void launch_step(TileShape t, const CUtensorMap& tm, const AcGeom& g, const AcStep& s,
+                        cudaStream_t st)
+{
+    if (t.warps == 8 && t.rpw == 4) launch_t<8, 4>(tm, g, s, st);
+    else if (t.warps == 4 && t.rpw == 8) launch_t<4, 8>(tm, g, s, st);
+    else if (t.warps == 8 && t.rpw == 8) launch_t<8, 8>(tm, g, s, st);
+    else if (t.warps == 4 && t.rpw == 4) launch_t<4, 4>(tm, g, s, st);
+    else launch_t<16, 4>(tm, g, s, st);
+}
+
+// ---- device buffer helper -------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;  // elements
+    int ensure(size_t n)
+    {
+        if (n <= cap) return W2D_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (n == 0) return W2D_OK;
+        cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error(std::string("device allocation failed: ") + cudaGetErrorString(e));
+            return W2D_ENOMEM;
+        }
+        cap = n;
+        return W2D_OK;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace w2d
+
+using namespace w2d;
+
+struct w2d_engine {
+    int nx = 0, nz = 0, ldx = 0, fs = 1;
+    float dx = 0, dz = 0, dt = 0;
+    float inv_dx2 = 0, inv_dz2 = 0, dt2 = 0;
+    size_t plane = 0;  // floats per pitched field
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    TileShape tile{8, 4};
+
+    int n_sponge = 0;
+    DevBuf<float> sponge_lut, sponge_arr;
+    bool use_lut = false, use_arr = false;
+
+    DevBuf<float> waves;  // 6 planes: forward triple then backward triple
+    CUtensorMap tm[6];
+    int tm_tz = -1;
+    DevBuf<float> v2dt2;  // 2 planes (slot 0 forward model, slot 1 backward model)
+    bool vel_set[2] = {false, false};
+    DevBuf<float> staging;  // one plane, pitched upload area
+
+    DevBuf<int> shot;  // {src_ix, src_iz, rec_iz}
+    DevBuf<int> rec_ptr, rec_list;
+    DevBuf<float> wavelet, data, rec_out;
+    DevBuf<float> snaps, ckpt;
+    DevBuf<float> image, illum, stack_img, stack_ill;
+    DevBuf<unsigned> err;
+    unsigned long long budget = 0;
+    // inputs of the pass being run (engine buffers or a staged slot)
+    const float* cur_w = nullptr;
+    const float* cur_data = nullptr;
+    // staged shot inputs (device-resident before a timed region)
+    std::vector<DevBuf<float>> st_w, st_d;
+    std::vector<int> st_nt, st_nrec;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+
+    // stats of the last call
+    int last_storage = 0;
+    long long last_launches = 0, last_recompute = 0;
+    float last_ms = 0.f;
+
+    float* wave(int i) { return waves.p + (size_t)i * plane; }
+};
+
+namespace {
+
+int upload_field(w2d_engine* e, float* dst_pitched, const float* host)
+{
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dst_pitched, (size_t)e->ldx * 4, host, (size_t)e->nx * 4,
+                                   (size_t)e->nx * 4, e->nz, cudaMemcpyHostToDevice, e->stream));
+    return W2D_OK;
+}
+
+int download_field(w2d_engine* e, float* host, const float* src_pitched)
+{
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(host, (size_t)e->nx * 4, src_pitched, (size_t)e->ldx * 4,
+                                   (size_t)e->nx * 4, e->nz, cudaMemcpyDeviceToHost, e->stream));
+    return W2D_OK;
+}
+
+int ensure_tensor_maps(w2d_engine* e)
+{
+    const int tz = e->tile.tz();
+    if (e->tm_tz == tz) return W2D_OK;
+    for (int i = 0; i < 6; ++i) {
+        int rc = make_tensor_map_2d(&e->tm[i], e->wave(i), e->nx, e->nz, e->ldx, AC_SW, tz + 4);
+        if (rc) return rc;
+    }
+    e->tm_tz = tz;
+    return W2D_OK;
+}
+
+AcGeom geom(w2d_engine* e)
+{
+    AcGeom g;
+    g.nx = e->nx;
+    g.nz = e->nz;
+    g.ldx = e->ldx;
+    g.inv_dx2 = e->inv_dx2;
+    g.inv_dz2 = e->inv_dz2;
+    g.free_surface = e->fs;
+    g.n_sponge = e->n_sponge;
+    g.sponge_lut = e->use_lut ? e->sponge_lut.p : nullptr;
+    g.sponge_arr = e->use_arr ? e->sponge_arr.p : nullptr;
+    g.rec_ptr = e->rec_ptr.p;
+    g.rec_list = e->rec_list.p;
+    g.shot = e->shot.p;
+    return g;
+}
+
+// Receivers: CSR by column, receivers of a column in index order.
+int set_shot(w2d_engine* e, int src_ix, int src_iz, const int* rec_ix, int n_rec, int rec_iz)
+{
+    W2D_CHECK_ARG(n_rec >= 0, "n_rec < 0");
+    W2D_CHECK_ARG(n_rec == 0 || rec_ix, "rec_ix is NULL");
+    W2D_CHECK_ARG(rec_iz >= 0 && rec_iz < e->nz, "receiver_iz out of range");
+    std::vector<int> ptr(e->nx + 1, 0), list(std::max(n_rec, 1));
+    for (int r = 0; r < n_rec; ++r) {
+        W2D_CHECK_ARG(rec_ix[r] >= 0 && rec_ix[r] < e->nx, "receiver_ix out of range");
+        ptr[rec_ix[r] + 1]++;
+    }
+    for (int i = 0; i < e->nx; ++i) ptr[i + 1] += ptr[i];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int r = 0; r < n_rec; ++r) list[fill[rec_ix[r]]++] = r;
+    int rc;
+    if ((rc = e->rec_ptr.ensure(e->nx + 1)) || (rc = e->rec_list.ensure(list.size())) ||
+        (rc = e->shot.ensure(4)))
+        return rc;
+    int sh[4] = {src_ix, src_iz, rec_iz, n_rec};
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_ptr.p, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
+                                 e->stream));
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_list.p, list.data(), list.size() * 4,
+                                 cudaMemcpyHostToDevice, e->stream));
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->shot.p, sh, sizeof sh, cudaMemcpyHostToDevice, e->stream));
+    // the host vectors die at return: wait for the copies
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return W2D_OK;
+}
+
+AcStep base_step(w2d_engine* e, int slot)
+{
+    AcStep s;
+    memset(&s, 0, sizeof s);
+    s.v2dt2 = e->v2dt2.p + (size_t)slot * e->plane;
+    s.dt2_inj = (float)((double)e->dt * (double)e->dt);
+    s.err = e->err.p;
+    return s;
+}
+
+// Forward steps [it0, it1) on the forward triple (roles by it % 3).
+struct FwdOpts {
+    int nt = 0, interval = 1, n_rec = 0;
+    float* rec_out = nullptr;    // (nt, n_rec) device
+    float* snaps = nullptr;      // snapshot slots, slot index = it/interval - slot0
+    int slot0 = 0;
+    bool illum = false;
+    float* ckpt = nullptr;       // save state every ckpt_every steps (3 planes per checkpoint)
+    int ckpt_every = 0;
+};
+
+int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it1, double dt2inj,
+                      float dt2inj_f)
+{
+    const AcGeom g = geom(e);
+    for (int it = it0; it < it1; ++it) {
+        float* prev = e->wave(it % 3);
+        float* curr = e->wave((it + 1) % 3);
+        float* next = e->wave((it + 2) % 3);
+        if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
+            float* c = o.ckpt + (size_t)(it / o.ckpt_every) * 3 * e->plane;
+            W2D_CUDA_TRY(cudaMemcpyAsync(c, prev, e->plane * 4, cudaMemcpyDeviceToDevice, e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(c + e->plane, curr, e->plane * 4, cudaMemcpyDeviceToDevice,
+                                         e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(c + 2 * e->plane, next, e->plane * 4,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+        }
+        AcStep s = base_step(e, slot);
+        s.p_prev = prev;
+        s.p_next = next;
+        s.dt2_inj = dt2inj_f;
+        if (it + 1 < o.nt) s.inj_w = e->cur_w + it + 1;
+        if (o.rec_out) s.rec_out = o.rec_out + (size_t)it * o.n_rec;
+        if (it % o.interval == 0) {
+            if (o.snaps) s.snap_out = o.snaps + (size_t)(it / o.interval - o.slot0) * e->plane;
+            if (o.illum) s.illum = e->illum.p;
+        }
+        launch_step(e->tile, e->tm[(it + 1) % 3], g, s, e->stream);
+        e->last_launches++;
+    }
+    (void)dt2inj;
+    W2D_CUDA_TRY(cudaGetLastError());
+    return W2D_OK;
+}
+
+int forward_begin(w2d_engine* e, float dt2inj_f)
+{
+    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(0), 0, 3 * e->plane * 4, e->stream));
+    const AcGeom g = geom(e);
+    inject_kernel<<<(e->nx + 255) / 256, 256, 0, e->stream>>>(e->wave(1), g, e->cur_w, nullptr,
+                                                              dt2inj_f);
+    e->last_launches++;
+    W2D_CUDA_TRY(cudaGetLastError());
+    return W2D_OK;
+}
+
+// Backward steps for it in [it_lo, it_hi] descending; m = nt-1-it picks roles
+// on the backward triple.  snaps: slot of step it = it/interval - slot0.
+int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec, int it_hi,
+                       int it_lo, const float* snaps, int slot0, int n_snaps_valid,
+                       float img_dt, float dt2inj_f)
+{
+    const AcGeom g = geom(e);
+    for (int it = it_hi; it >= it_lo; --it) {
+        const int m = nt - 1 - it;
+        float* prev = e->wave(3 + m % 3);
+        float* next = e->wave(3 + (m + 2) % 3);
+        AcStep s = base_step(e, slot);
+        s.p_prev = prev;
+        s.p_next = next;
+        s.dt2_inj = dt2inj_f;
+        if (it >= 1 && n_rec > 0) s.inj_data = e->cur_data + (size_t)(it - 1) * n_rec;
+        if (snaps && it % interval == 0) {
+            const int k = it / interval;
+            if (k >= 0 && k < n_snaps_valid) {
+                s.snap_in = snaps + (size_t)(k - slot0) * e->plane;
+                s.image = e->image.p;
+                s.img_dt = img_dt;
+            }
+        }
+        launch_step(e->tile, e->tm[3 + (m + 1) % 3], g, s, e->stream);
+        e->last_launches++;
+    }
+    W2D_CUDA_TRY(cudaGetLastError());
+    return W2D_OK;
+}
+
+int backward_begin(w2d_engine* e, int nt, int n_rec, float dt2inj_f)
+{
+    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * e->plane * 4, e->stream));
+    const AcGeom g = geom(e);
+    inject_kernel<<<(e->nx + 255) / 256, 256, 0, e->stream>>>(
+        e->wave(4), g, nullptr, e->cur_data + (size_t)(nt - 1) * n_rec, dt2inj_f);
+    e->last_launches++;
+    W2D_CUDA_TRY(cudaGetLastError());
+    return W2D_OK;
+}
+
+int check_err(w2d_engine* e)
+{
+    unsigned h = 0;
+    W2D_CUDA_TRY(cudaMemcpyAsync(&h, e->err.p, 4, cudaMemcpyDeviceToHost, e->stream));
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    if (h) {
+        char buf[96];
+        snprintf(buf, sizeof buf, "device wait gave up (error bits 0x%x)", h);
+        set_error(buf);
+        W2D_CUDA_TRY(cudaMemsetAsync(e->err.p, 0, 4, e->stream));
+        return W2D_ETIMEOUT;
+    }
+    return W2D_OK;
+}
+
+int common_checks(w2d_engine* e, int nt, int interval)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CHECK_ARG(nt > 0, "nt must be positive");
+    W2D_CHECK_ARG(interval > 0, "snapshot_interval must be positive");
+    return W2D_OK;
+}
+
+size_t free_budget(w2d_engine* e)
+{
+    if (e->budget) return (size_t)e->budget;
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    return (size_t)(fr * 0.8);
+}
+
+}  // namespace
+
+extern "C" {
+
+int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, float dt,
+                      const float* sponge, int free_surface_top)
+{
+    W2D_CHECK_ARG(out, "out is NULL");
+    *out = nullptr;
+    W2D_CHECK_ARG(nx >= 5 && nz >= 5, "grid must be at least 5 x 5");
+    W2D_CHECK_ARG(dx > 0 && dz > 0 && dt > 0, "dx, dz, dt must be positive");
+    w2d_engine* e = new w2d_engine();
+    e->nx = nx;
+    e->nz = nz;
+    e->ldx = pitch_for(nx);
+    e->plane = (size_t)e->ldx * nz;
+    e->dx = dx;
+    e->dz = dz;
+    e->dt = dt;
+    e->fs = free_surface_top ? 1 : 0;
+    e->inv_dx2 = 1.0f / (dx * dx);
+    e->inv_dz2 = 1.0f / (dz * dz);
+    e->dt2 = dt * dt;
+    int rc = W2D_OK;
+    auto fail = [&](int code) {
+        w2d_engine_destroy(e);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
+        set_error("stream/event creation failed");
+        return fail(W2D_ECUDA);
+    }
+    if ((rc = e->waves.ensure(6 * e->plane)) || (rc = e->v2dt2.ensure(2 * e->plane)) ||
+        (rc = e->staging.ensure(e->plane)) || (rc = e->image.ensure(e->plane)) ||
+        (rc = e->illum.ensure(e->plane)) || (rc = e->err.ensure(1)))
+        return fail(rc);
+    if (cudaMemset(e->err.p, 0, 4) != cudaSuccess || cudaMemset(e->waves.p, 0, 6 * e->plane * 4) ||
+        cudaMemset(e->v2dt2.p, 0, 2 * e->plane * 4)) {
+        set_error("memset failed");
+        return fail(W2D_ECUDA);
+    }
+    // Sponge: a Cerjan table when the array is one, else the array itself.
+    if (sponge) {
+        // recover (n, alpha) candidates from the array: n is the largest frame
+        // distance with a value != 1; alpha from the value at distance 1 is not
+        // needed, the table is rebuilt from the array's own values and verified.
+        int nmax = std::max(nx, nz);
+        std::vector<float> lut(nmax + 2, 1.0f);
+        std::vector<char> seen(nmax + 2, 0);
+        bool ok = true;
+        int n_est = -1;
+        // distances with respect to every candidate n are not known yet; probe along
+        // row nz/2 from the left edge: d = n - ix for ix < n.
+        const float* mid = sponge + (size_t)(nz / 2) * nx;
+        for (int ix = 0; ix < nx && mid[ix] != 1.0f; ++ix) n_est = ix + 1;
+        // n_est: count of non-unit cells from the left; d = n - ix > 0 for ix < n.
+        const int n = n_est < 0 ? 0 : n_est;
+        for (int iz = 0; iz < nz && ok; ++iz)
+            for (int ix = 0; ix < nx; ++ix) {
+                int d = 0;
+                d = std::max(d, n - ix);
+                d = std::max(d, ix - (nx - 1 - n));
+                d = std::max(d, iz - (nz - 1 - n));
+                if (!free_surface_top) d = std::max(d, n - iz);
+                const float v = sponge[(size_t)iz * nx + ix];
+                if (d == 0) {
+                    if (v != 1.0f) { ok = false; break; }
+                } else if (!seen[d]) {
+                    seen[d] = 1;
+                    lut[d] = v;
+                } else if (lut[d] != v) {
+                    ok = false;
+                    break;
+                }
+            }
+        if (ok) {
+            e->n_sponge = n;
+            lut[0] = 1.0f;
+            if ((rc = e->sponge_lut.ensure(n + 1))) return fail(rc);
+            cudaMemcpy(e->sponge_lut.p, lut.data(), (n + 1) * 4, cudaMemcpyHostToDevice);
+            e->use_lut = true;
+        } else {
+            if ((rc = e->sponge_arr.ensure(e->plane))) return fail(rc);
+            cudaMemset(e->sponge_arr.p, 0, e->plane * 4);
+            cudaMemcpy2D(e->sponge_arr.p, (size_t)e->ldx * 4, sponge, (size_t)nx * 4,
+                         (size_t)nx * 4, nz, cudaMemcpyHostToDevice);
+            e->use_arr = true;
+        }
+    }
+    if ((rc = e->shot.ensure(4)) || (rc = e->rec_ptr.ensure(nx + 1)) ||
+        (rc = e->rec_list.ensure(1)))
+        return fail(rc);
+    int sh[4] = {-1, -1, -1, 0};
+    cudaMemcpy(e->shot.p, sh, sizeof sh, cudaMemcpyHostToDevice);
+    cudaMemset(e->rec_ptr.p, 0, (nx + 1) * 4);
+    if ((rc = ensure_tensor_maps(e))) return fail(rc);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        set_error("engine set-up failed");
+        return fail(W2D_ECUDA);
+    }
+    *out = e;
+    return W2D_OK;
+}
+
+void w2d_engine_destroy(w2d_engine* e)
+{
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (DevBuf<float>* b : {&e->sponge_lut, &e->sponge_arr, &e->waves, &e->v2dt2, &e->staging,
+                             &e->wavelet, &e->data, &e->rec_out, &e->snaps, &e->ckpt, &e->image,
+                             &e->illum, &e->stack_img, &e->stack_ill})
+        b->release();
+    e->shot.release();
+    e->rec_ptr.release();
+    e->rec_list.release();
+    e->err.release();
+    for (auto& b : e->st_w) b.release();
+    for (auto& b : e->st_d) b.release();
+    if (e->t0) cudaEventDestroy(e->t0);
+    if (e->t1) cudaEventDestroy(e->t1);
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    if (warps == 0 && rows_per_warp == 0) {
+        warps = 8;
+        rows_per_warp = 4;
+    }
+    W2D_CHECK_ARG(tile_supported(warps, rows_per_warp), "unsupported tile shape");
+    e->tile = TileShape{warps, rows_per_warp};
+    return ensure_tensor_maps(e);
+}
+
+int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    e->budget = bytes;
+    return W2D_OK;
+}
+
+int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel)
+{
+    W2D_CHECK_ARG(e && vel, "NULL argument");
+    W2D_CHECK_ARG(slot == 0 || slot == 1, "velocity slot must be 0 or 1");
+    int rc;
+    W2D_CUDA_TRY(cudaMemsetAsync(e->staging.p, 0, e->plane * 4, e->stream));
+    if ((rc = upload_field(e, e->staging.p, vel))) return rc;
+    v2dt2_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->v2dt2.p + (size_t)slot * e->plane,
+                                                            e->staging.p, e->plane, e->dt2);
+    W2D_CUDA_TRY(cudaGetLastError());
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->vel_set[slot] = true;
+    return W2D_OK;
+}
+
+int w2d_forward(w2d_engine* e, int vel_slot, const float* wavelet, int nt, int src_ix, int src_iz,
+                const int* rec_ix, int n_rec, int rec_iz, float* rec_out, float* snaps_out,
+                int snapshot_interval)
+{
+    int rc;
+    if ((rc = common_checks(e, nt, snapshot_interval))) return rc;
+    W2D_CHECK_ARG(vel_slot == 0 || vel_slot == 1, "bad velocity slot");
+    W2D_CHECK_ARG(e->vel_set[vel_slot], "velocity model not set");
+    W2D_CHECK_ARG(wavelet, "wavelet is NULL");
+    W2D_CHECK_ARG(src_ix >= 0 && src_ix < e->nx && src_iz >= 0 && src_iz < e->nz,
+                  "source index out of range");
+    if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
+    const int n_snaps = snaps_out ? (nt - 1) / snapshot_interval + 1 : 0;
+    if ((rc = e->wavelet.ensure(nt)) || (rc = e->rec_out.ensure((size_t)nt * std::max(n_rec, 1))))
+        return rc;
+    if (snaps_out) {
+        const size_t need = (size_t)n_snaps * e->plane;
+        if (need * 4 > free_budget(e) + e->snaps.cap * 4) {
+            set_error("snapshot storage exceeds the device memory budget");
+            return W2D_ENOMEM;
+        }
+        if ((rc = e->snaps.ensure(need))) return rc;
+    }
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet.p, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice,
+                                 e->stream));
+    e->cur_w = e->wavelet.p;
+    e->last_launches = 0;
+    e->last_recompute = 0;
+    e->last_storage = 0;
+    const float dt2inj = (float)((double)e->dt * (double)e->dt);
+    cudaEventRecord(e->ev0, e->stream);
+    if ((rc = forward_begin(e, dt2inj))) return rc;
+    FwdOpts o;
+    o.nt = nt;
+    o.interval = snapshot_interval;
+    o.n_rec = n_rec;
+    o.rec_out = n_rec > 0 ? e->rec_out.p : nullptr;
+    o.snaps = snaps_out ? e->snaps.p : nullptr;
+    if ((rc = run_forward_steps(e, vel_slot, o, 0, nt, 0.0, dt2inj))) return rc;
+    cudaEventRecord(e->ev1, e->stream);
+    if (n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(rec_out, e->rec_out.p, (size_t)nt * n_rec * 4,
+                                     cudaMemcpyDeviceToHost, e->stream));
+    for (int k = 0; k < n_snaps; ++k)
+        if ((rc = download_field(e, snaps_out + (size_t)k * e->nx * e->nz,
+                                 e->snaps.p + (size_t)k * e->plane)))
+            return rc;
+    if ((rc = check_err(e))) return rc;
+    cudaEventElapsedTime(&e->last_ms, e->ev0, e->ev1);
+    return W2D_OK;
+}
+
+int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int nt,
+                           const int* rec_ix, int n_rec, int rec_iz, const float* fwd_snaps,
+                           int n_snaps, float* image, int snapshot_interval)
+{
+    int rc;
+    if ((rc = common_checks(e, nt, snapshot_interval))) return rc;
+    W2D_CHECK_ARG(vel_slot == 0 || vel_slot == 1, "bad velocity slot");
+    W2D_CHECK_ARG(e->vel_set[vel_slot], "velocity model not set");
+    W2D_CHECK_ARG(image, "image is NULL");
+    W2D_CHECK_ARG(n_rec == 0 || data, "data is NULL");
+    W2D_CHECK_ARG(n_snaps >= 0 && (n_snaps == 0 || fwd_snaps), "bad forward wavefields");
+    if ((rc = set_shot(e, -1, -1, rec_ix, n_rec, rec_iz))) return rc;
+    // The reference correlates only while its snapshot counter, which starts at
+    // (nt-1)/interval, indexes an existing snapshot (wave_solver.py:204,230): with
+    // fewer snapshots it never correlates.
+    if (n_snaps <= (nt - 1) / snapshot_interval) n_snaps = 0;
+    if ((rc = e->data.ensure((size_t)nt * std::max(n_rec, 1)))) return rc;
+    if (n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, data, (size_t)nt * n_rec * 4,
+                                     cudaMemcpyHostToDevice, e->stream));
+    if (n_snaps > 0) {
+        const size_t need = (size_t)n_snaps * e->plane;
+        if (need * 4 > free_budget(e) + e->snaps.cap * 4) {
+            set_error("forward wavefields exceed the device memory budget");
+            return W2D_ENOMEM;
+        }
+        if ((rc = e->snaps.ensure(need))) return rc;
+        W2D_CUDA_TRY(cudaMemsetAsync(e->snaps.p, 0, need * 4, e->stream));
+        for (int k = 0; k < n_snaps; ++k)
+            if ((rc = upload_field(e, e->snaps.p + (size_t)k * e->plane,
+                                   fwd_snaps + (size_t)k * e->nx * e->nz)))
+                return rc;
+    }
+    W2D_CUDA_TRY(cudaMemsetAsync(e->image.p, 0, e->plane * 4, e->stream));
+    if ((rc = upload_field(e, e->image.p, image))) return rc;
+    e->cur_data = e->data.p;
+    e->last_launches = 0;
+    e->last_recompute = 0;
+    const float dt2inj = (float)((double)e->dt * (double)e->dt);
+    const float img_dt = (float)((double)e->dt * (double)snapshot_interval);
+    cudaEventRecord(e->ev0, e->stream);
+    if (n_rec > 0) {
+        if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
+    } else {
+        W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * e->plane * 4, e->stream));
+    }
+    if ((rc = run_backward_steps(e, vel_slot, nt, snapshot_interval, n_rec, nt - 1, 0,
+                                 n_snaps > 0 ? e->snaps.p : nullptr, 0, n_snaps, img_dt, dt2inj)))
+        return rc;
+    cudaEventRecord(e->ev1, e->stream);
+    if ((rc = download_field(e, image, e->image.p))) return rc;
+    if ((rc = check_err(e))) return rc;
+    cudaEventElapsedTime(&e->last_ms, e->ev0, e->ev1);
+    return W2D_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Forward + backward migration of one shot whose wavelet and data are already
+// on the device (e->cur_w, e->cur_data) and whose geometry is set.
+int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int storage,
+                 float* image_out, float* illum_out)
+{
+    int rc;
+    const int interval = snapshot_interval;
+    const int n_snaps = (nt - 1) / interval + 1;
+    const size_t plane_b = e->plane * 4;
+
+    // storage decision
+    const size_t full_bytes = (size_t)n_snaps * plane_b;
+    const size_t budget = free_budget(e) + e->snaps.cap * 4 + e->ckpt.cap * 4;
+    int mode = storage;
+    if (mode == W2D_STORE_AUTO) mode = full_bytes <= budget ? W2D_STORE_ALL : W2D_STORE_CHECKPOINT;
+    W2D_CHECK_ARG(mode == W2D_STORE_ALL || mode == W2D_STORE_CHECKPOINT, "bad storage mode");
+    int seg = 0, n_seg = 0;
+    if (mode == W2D_STORE_ALL) {
+        if (full_bytes > budget) {
+            set_error("full snapshot storage exceeds the device memory budget");
+            return W2D_ENOMEM;
+        }
+        if ((rc = e->snaps.ensure((size_t)n_snaps * e->plane))) return rc;
+    } else {
+        // segment length: about sqrt(3 * nt * interval) steps, rounded to the interval,
+        // balancing 3-plane checkpoints against the snapshots of one segment.
+        seg = (int)std::max(1.0, std::sqrt(3.0 * nt * interval));
+        seg = std::max(interval, (seg / interval) * interval);
+        n_seg = (nt + seg - 1) / seg;
+        const int seg_snaps = seg / interval + 1;
+        const size_t need = ((size_t)n_seg * 3 + seg_snaps) * plane_b;
+        if (need > budget) {
+            set_error("checkpoint storage exceeds the device memory budget");
+            return W2D_ENOMEM;
+        }
+        if ((rc = e->ckpt.ensure((size_t)n_seg * 3 * e->plane)) ||
+            (rc = e->snaps.ensure((size_t)seg_snaps * e->plane)))
+            return rc;
+    }
+    e->last_launches = 0;
+    e->last_recompute = 0;
+    e->last_storage = mode;
+    const float dt2inj = (float)((double)e->dt * (double)e->dt);
+    const float img_dt = (float)((double)e->dt * (double)interval);
+    cudaEventRecord(e->ev0, e->stream);
+    W2D_CUDA_TRY(cudaMemsetAsync(e->illum.p, 0, plane_b, e->stream));
+    W2D_CUDA_TRY(cudaMemsetAsync(e->image.p, 0, plane_b, e->stream));
+
+    // 1. forward pass in slot 0 with illumination
+    if ((rc = forward_begin(e, dt2inj))) return rc;
+    FwdOpts o;
+    o.nt = nt;
+    o.interval = interval;
+    o.illum = true;
+    if (mode == W2D_STORE_ALL) {
+        o.snaps = e->snaps.p;
+    } else {
+        o.ckpt = e->ckpt.p;
+        o.ckpt_every = seg;
+    }
+    if ((rc = run_forward_steps(e, 0, o, 0, nt, 0.0, dt2inj))) return rc;
+    scale_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->illum.p, e->plane, img_dt);
+    e->last_launches++;
+
+    // 2. backward pass in slot 1 with imaging
+    if (n_rec > 0) {
+        if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
+    } else {
+        W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * plane_b, e->stream));
+    }
+    if (mode == W2D_STORE_ALL) {
+        if ((rc = run_backward_steps(e, 1, nt, interval, n_rec, nt - 1, 0, e->snaps.p, 0, n_snaps,
+                                     img_dt, dt2inj)))
+            return rc;
+    } else {
+        for (int sgi = n_seg - 1; sgi >= 0; --sgi) {
+            const int a = sgi * seg, b = std::min(nt, a + seg);
+            // restore the forward state at step a and recompute [a, b) with snapshots
+            const float* c = e->ckpt.p + (size_t)sgi * 3 * e->plane;
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave(a % 3), c, plane_b, cudaMemcpyDeviceToDevice,
+                                         e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 1) % 3), c + e->plane, plane_b,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 2) % 3), c + 2 * e->plane, plane_b,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            FwdOpts r;
+            r.nt = nt;
+            r.interval = interval;
+            r.snaps = e->snaps.p;
+            r.slot0 = (a + interval - 1) / interval;  // first snapshot index in [a, b)
+            if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
+            e->last_recompute += b - a;
+            if ((rc = run_backward_steps(e, 1, nt, interval, n_rec, b - 1, a, e->snaps.p, r.slot0,
+                                         n_snaps, img_dt, dt2inj)))
+                return rc;
+        }
+    }
+    cudaEventRecord(e->ev1, e->stream);
+    if (image_out) {
+        if ((rc = download_field(e, image_out, e->image.p)) ||
+            (rc = download_field(e, illum_out, e->illum.p)))
+            return rc;
+    } else {
+        if ((rc = e->stack_img.ensure(e->plane)) || (rc = e->stack_ill.ensure(e->plane))) return rc;
+        add_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->stack_img.p, e->image.p, e->plane);
+        add_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->stack_ill.p, e->illum.p, e->plane);
+        e->last_launches += 2;
+        W2D_CUDA_TRY(cudaGetLastError());
+    }
+    if ((rc = check_err(e))) return rc;
+    cudaEventElapsedTime(&e->last_ms, e->ev0, e->ev1);
+    return W2D_OK;
+}
+
+int migrate_checks(w2d_engine* e, int nt, int interval, int src_ix, int src_iz, int n_rec,
+                   float* image_out, float* illum_out)
+{
+    int rc;
+    if ((rc = common_checks(e, nt, interval))) return rc;
+    W2D_CHECK_ARG(e->vel_set[0] && e->vel_set[1], "velocity models not set");
+    W2D_CHECK_ARG(n_rec >= 0, "n_rec < 0");
+    W2D_CHECK_ARG(src_ix >= 0 && src_ix < e->nx && src_iz >= 0 && src_iz < e->nz,
+                  "source index out of range");
+    W2D_CHECK_ARG((image_out == nullptr) == (illum_out == nullptr),
+                  "image_out and illum_out must both be set or both be NULL");
+    return W2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, int src_iz,
+                     const float* data, const int* rec_ix, int n_rec, int rec_iz,
+                     int snapshot_interval, int storage, float* image_out, float* illum_out)
+{
+    int rc;
+    if ((rc = migrate_checks(e, nt, snapshot_interval, src_ix, src_iz, n_rec, image_out,
+                             illum_out)))
+        return rc;
+    W2D_CHECK_ARG(wavelet, "wavelet is NULL");
+    W2D_CHECK_ARG(n_rec == 0 || data, "data is NULL");
+    if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
+    if ((rc = e->wavelet.ensure(nt)) || (rc = e->data.ensure((size_t)nt * std::max(n_rec, 1))))
+        return rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet.p, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice,
+                                 e->stream));
+    if (n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, data, (size_t)nt * n_rec * 4,
+                                     cudaMemcpyHostToDevice, e->stream));
+    e->cur_w = e->wavelet.p;
+    e->cur_data = e->data.p;
+    return migrate_core(e, nt, n_rec, snapshot_interval, storage, image_out, illum_out);
+}
+
+int w2d_shot_stage(w2d_engine* e, int slot, const float* wavelet, int nt, const float* data,
+                   int n_rec)
+{
+    W2D_CHECK_ARG(e && wavelet && nt > 0 && slot >= 0 && slot < 4096, "bad arguments");
+    W2D_CHECK_ARG(n_rec >= 0 && (n_rec == 0 || data), "bad data");
+    if ((int)e->st_w.size() <= slot) {
+        e->st_w.resize(slot + 1);
+        e->st_d.resize(slot + 1);
+        e->st_nt.resize(slot + 1, 0);
+        e->st_nrec.resize(slot + 1, 0);
+    }
+    int rc;
+    if ((rc = e->st_w[slot].ensure(nt)) ||
+        (rc = e->st_d[slot].ensure((size_t)nt * std::max(n_rec, 1))))
+        return rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->st_w[slot].p, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice,
+                                 e->stream));
+    if (n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->st_d[slot].p, data, (size_t)nt * n_rec * 4,
+                                     cudaMemcpyHostToDevice, e->stream));
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->st_nt[slot] = nt;
+    e->st_nrec[slot] = n_rec;
+    return W2D_OK;
+}
+
+int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const int* rec_ix,
+                       int n_rec, int rec_iz, int snapshot_interval, int storage,
+                       float* image_out, float* illum_out)
+{
+    W2D_CHECK_ARG(e && slot >= 0 && slot < (int)e->st_nt.size() && e->st_nt[slot] > 0,
+                  "slot not staged");
+    W2D_CHECK_ARG(n_rec == e->st_nrec[slot], "n_rec differs from the staged data");
+    const int nt = e->st_nt[slot];
+    int rc;
+    if ((rc = migrate_checks(e, nt, snapshot_interval, src_ix, src_iz, n_rec, image_out,
+                             illum_out)))
+        return rc;
+    if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
+    e->cur_w = e->st_w[slot].p;
+    e->cur_data = e->st_d[slot].p;
+    return migrate_core(e, nt, n_rec, snapshot_interval, storage, image_out, illum_out);
+}
+
+int w2d_engine_timer_start(w2d_engine* e)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    if (!e->t0 && (cudaEventCreate(&e->t0) != cudaSuccess || cudaEventCreate(&e->t1) != cudaSuccess)) {
+        set_error("event creation failed");
+        return W2D_ECUDA;
+    }
+    W2D_CUDA_TRY(cudaEventRecord(e->t0, e->stream));
+    return W2D_OK;
+}
+
+int w2d_engine_timer_stop(w2d_engine* e, float* ms)
+{
+    W2D_CHECK_ARG(e && e->t0 && ms, "timer not started");
+    W2D_CUDA_TRY(cudaEventRecord(e->t1, e->stream));
+    W2D_CUDA_TRY(cudaEventSynchronize(e->t1));
+    W2D_CUDA_TRY(cudaEventElapsedTime(ms, e->t0, e->t1));
+    return W2D_OK;
+}
+
+int w2d_host_alloc(void** out, unsigned long long bytes)
+{
+    W2D_CHECK_ARG(out, "out is NULL");
+    W2D_CUDA_TRY(cudaMallocHost(out, (size_t)bytes));
+    return W2D_OK;
+}
+
+void w2d_host_free(void* p)
+{
+    if (p) cudaFreeHost(p);
+}
+
+int w2d_stack_reset(w2d_engine* e)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    int rc;
+    if ((rc = e->stack_img.ensure(e->plane)) || (rc = e->stack_ill.ensure(e->plane))) return rc;
+    W2D_CUDA_TRY(cudaMemsetAsync(e->stack_img.p, 0, e->plane * 4, e->stream));
+    W2D_CUDA_TRY(cudaMemsetAsync(e->stack_ill.p, 0, e->plane * 4, e->stream));
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return W2D_OK;
+}
+
+int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out)
+{
+    W2D_CHECK_ARG(e && image_out && illum_out, "NULL argument");
+    W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
+    int rc;
+    if ((rc = download_field(e, image_out, e->stack_img.p)) ||
+        (rc = download_field(e, illum_out, e->stack_ill.p)))
+        return rc;
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return W2D_OK;
+}
+
+int w2d_engine_last_stats(w2d_engine* e, int* storage_used, long long* step_launches,
+                          long long* recomputed_steps, float* device_ms)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    if (storage_used) *storage_used = e->last_storage;
+    if (step_launches) *step_launches = e->last_launches;
+    if (recomputed_steps) *recomputed_steps = e->last_recompute;
+    if (device_ms) *device_ms = e->last_ms;
+    return W2D_OK;
+}
+
+// ---- reference-compatible per-step entry points ------------------------------
+
+static std::mutex g_legacy_mu;
+static struct {
+    int nx = 0, nz = 0, ldx = 0;
+    DevBuf<float> buf;  // p_curr, p_prev, p_next, v2dt2, sponge, vel staging
+    DevBuf<int> shot, rec_ptr;
+    DevBuf<unsigned> err;
+    CUtensorMap tm;
+    cudaStream_t stream = nullptr;
+} g_leg;
+
+static int legacy_prepare(int nx, int nz)
+{
+    if (!g_leg.stream && cudaStreamCreateWithFlags(&g_leg.stream, cudaStreamNonBlocking)) {
+        set_error("stream creation failed");
+        return W2D_ECUDA;
+    }
+    const int ldx = pitch_for(nx);
+    const size_t plane = (size_t)ldx * nz;
+    int rc;
+    if ((rc = g_leg.shot.ensure(4)) || (rc = g_leg.err.ensure(1))) return rc;
+    if (g_leg.nx != nx || g_leg.nz != nz) {
+        if ((rc = g_leg.buf.ensure(6 * plane)) || (rc = g_leg.rec_ptr.ensure(nx + 1))) return rc;
+        W2D_CUDA_TRY(cudaMemset(g_leg.buf.p, 0, 6 * plane * 4));
+        W2D_CUDA_TRY(cudaMemset(g_leg.rec_ptr.p, 0, (nx + 1) * 4));
+        int sh[4] = {-1, -1, -1, 0};
+        W2D_CUDA_TRY(cudaMemcpy(g_leg.shot.p, sh, sizeof sh, cudaMemcpyHostToDevice));
+        W2D_CUDA_TRY(cudaMemset(g_leg.err.p, 0, 4));
+        if ((rc = make_tensor_map_2d(&g_leg.tm, g_leg.buf.p, nx, nz, ldx, AC_SW, 32 + 4))) return rc;
+        g_leg.nx = nx;
+        g_leg.nz = nz;
+        g_leg.ldx = ldx;
+    }
+    return W2D_OK;
+}
+
+static int legacy_acoustic(const float* p_curr, const float* p_prev, float* p_next,
+                           const float* vel, const float* sponge, int nx, int nz, float dx,
+                           float dz, float dt, int fs)
+{
+    W2D_CHECK_ARG(p_curr && p_prev && p_next && vel, "NULL field");
+    W2D_CHECK_ARG(nx >= 5 && nz >= 5, "grid must be at least 5 x 5");
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    int rc;
+    if ((rc = legacy_prepare(nx, nz))) return rc;
+    const int ldx = g_leg.ldx;
+    const size_t plane = (size_t)ldx * nz;
+    float* d = g_leg.buf.p;
+    float *dc = d, *dp = d + plane, *dn = d + 2 * plane, *dv = d + 3 * plane, *ds = d + 4 * plane,
+          *dvel = d + 5 * plane;
+    cudaStream_t st = g_leg.stream;
+    const size_t hp = (size_t)nx * 4, dp_b = (size_t)ldx * 4;
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dc, dp_b, p_curr, hp, hp, nz, cudaMemcpyHostToDevice, st));
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dp, dp_b, p_prev, hp, hp, nz, cudaMemcpyHostToDevice, st));
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dn, dp_b, p_next, hp, hp, nz, cudaMemcpyHostToDevice, st));
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dvel, dp_b, vel, hp, hp, nz, cudaMemcpyHostToDevice, st));
+    if (sponge)
+        W2D_CUDA_TRY(cudaMemcpy2DAsync(ds, dp_b, sponge, hp, hp, nz, cudaMemcpyHostToDevice, st));
+    v2dt2_kernel<<<grid_for(plane), 256, 0, st>>>(dv, dvel, plane, dt * dt);
+    AcGeom g;
+    memset(&g, 0, sizeof g);
+    g.nx = nx;
+    g.nz = nz;
+    g.ldx = ldx;
+    g.inv_dx2 = 1.0f / (dx * dx);
+    g.inv_dz2 = 1.0f / (dz * dz);
+    g.free_surface = fs ? 1 : 0;
+    g.sponge_arr = sponge ? ds : nullptr;
+    g.rec_ptr = g_leg.rec_ptr.p;
+    g.rec_list = g_leg.rec_ptr.p;
+    g.shot = g_leg.shot.p;
+    AcStep s;
+    memset(&s, 0, sizeof s);
+    s.p_prev = dp;
+    s.p_next = dn;
+    s.v2dt2 = dv;
+    s.err = g_leg.err.p;
+    launch_t<8, 4>(g_leg.tm, g, s, st);
+    W2D_CUDA_TRY(cudaGetLastError());
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(p_next, hp, dn, dp_b, hp, nz, cudaMemcpyDeviceToHost, st));
+    unsigned h = 0;
+    W2D_CUDA_TRY(cudaMemcpyAsync(&h, g_leg.err.p, 4, cudaMemcpyDeviceToHost, st));
+    W2D_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h) {
+        cudaMemset(g_leg.err.p, 0, 4);
+        set_error("device wait gave up in acoustic_2d_step");
+        return W2D_ETIMEOUT;
+    }
+    return W2D_OK;
+}
+
+void acoustic_2d_step(const float* p_curr, const float* p_prev, float* p_next, const float* vel,
+                      const float* sponge, int nx, int nz, float dx, float dz, float dt,
+                      int free_surface_top)
+{
+    legacy_acoustic(p_curr, p_prev, p_next, vel, sponge, nx, nz, dx, dz, dt, free_surface_top);
+}
+
+int w2d_acoustic_2d_step_status(const float* p_curr, const float* p_prev, float* p_next,
+                                const float* vel, const float* sponge, int nx, int nz, float dx,
+                                float dz, float dt, int free_surface_top)
+{
+    return legacy_acoustic(p_curr, p_prev, p_next, vel, sponge, nx, nz, dx, dz, dt,
+                           free_surface_top);
+}
+
+static int legacy_correlate(const float* src, const float* rec, float* image, int nx, int nz,
+                            float dt)
+{
+    W2D_CHECK_ARG(src && rec && image && nx > 0 && nz > 0, "bad arguments");
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    static DevBuf<float> buf;
+    static cudaStream_t st = nullptr;
+    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) {
+        set_error("stream creation failed");
+        return W2D_ECUDA;
+    }
+    const size_t n = (size_t)nx * nz;
+    int rc;
+    if ((rc = buf.ensure(3 * n))) return rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p, src, n * 4, cudaMemcpyHostToDevice, st));
+    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p + n, rec, n * 4, cudaMemcpyHostToDevice, st));
+    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p + 2 * n, image, n * 4, cudaMemcpyHostToDevice, st));
+    correlate_kernel<<<grid_for(n), 256, 0, st>>>(buf.p, buf.p + n, buf.p + 2 * n, n, dt);
+    W2D_CUDA_TRY(cudaGetLastError());
+    W2D_CUDA_TRY(cudaMemcpyAsync(image, buf.p + 2 * n, n * 4, cudaMemcpyDeviceToHost, st));
+    W2D_CUDA_TRY(cudaStreamSynchronize(st));
+    return W2D_OK;
+}
+
+void correlate_imaging_condition(const float* src_wavefield, const float* rec_wavefield,
+                                 float* image, int nx, int nz, float dt)
+{
+    legacy_correlate(src_wavefield, rec_wavefield, image, nx, nz, dt);
+}
+
+int w2d_correlate_status(const float* src, const float* rec, float* image, int nx, int nz,
+                         float dt)
+{
+    return legacy_correlate(src, rec, image, nx, nz, dt);
+}
+
+}  // extern "C"

@@ -1,0 +1,129 @@
+// w2d_common.cuh -- shared device/host helpers for the GB300 wave engine.
+//
+// Device memory layout used by every kernel in this library: a wavefield of
+// nz rows by nx columns is stored row-major with a row pitch `ldx` (floats) that
+// is a multiple of 32, so that every row starts on a 128-byte boundary, every
+// float4 of a row is 16-byte aligned, and a TMA tensor map can describe the
+// array (strides must be multiples of 16 bytes).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "wave2d_cuda.h"
+
+namespace w2d {
+
+// Status codes returned across the C ABI are the W2D_* values of wave2d_cuda.h.
+
+void set_error(const std::string& msg);
+const char* last_error();
+
+#define W2D_CUDA_TRY(expr)                                                             \
+    do {                                                                               \
+        cudaError_t _e = (expr);                                                       \
+        if (_e != cudaSuccess) {                                                       \
+            ::w2d::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));      \
+            return W2D_ECUDA;                                                   \
+        }                                                                              \
+    } while (0)
+
+#define W2D_CHECK_ARG(cond, msg)                                                       \
+    do {                                                                               \
+        if (!(cond)) {                                                                 \
+            ::w2d::set_error(msg);                                                     \
+            return W2D_EINVAL;                                                  \
+        }                                                                              \
+    } while (0)
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+inline int pitch_for(int nx) { return round_up(nx, 32); }
+
+// Device error-flag bits (written by kernels, read by the host after a pass).
+enum ErrBits : unsigned {
+    ERR_TMA_TIMEOUT = 1u,
+};
+
+// ---- PTX helpers (sm_100+ family; compiled for sm_103a) ---------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.  Returns false (and the caller records an
+// error bit) if the phase did not complete within `max_polls` polls; every
+// try_wait suspends the thread for a hardware-defined slice, so the bound is a
+// time bound of well under a second for the sizes used here.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint32_t max_polls = (1u << 22))
+{
+    for (uint32_t i = 0; i < max_polls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// 2D tiled TMA load of one box into shared memory, completion signalled on `bar`.
+// The innermost coordinate x must be a multiple of 4 floats (16 bytes).
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map)
+{
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// IEEE single-precision arithmetic with no contraction into FMA: the engine
+// evaluates every stencil in the reference's operation order so that float32
+// results are bit-identical to the reference C engine built without FMA.
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
+// Host: encode a 2D fp32 tensor map over a pitched array (nz rows of nx valid
+// floats, row pitch ldx floats) with a box of box_x by box_z elements.  Reads
+// outside [0,nx) x [0,nz) return zero.
+int make_tensor_map_2d(CUtensorMap* out, const float* base, int nx, int nz, int ldx, int box_x,
+                       int box_z);
+
+}  // namespace w2d

@@ -1,0 +1,161 @@
+/*
+ * wave2d_cuda.h -- C ABI of the GB300 (sm_103a) 2D wave / RTM engine.
+ *
+ * Library: das_gb300/libwave2d_cuda.so.  Arrays are C-contiguous float32
+ * (nz rows of nx) in HOST memory unless a name says otherwise; the library
+ * moves them to and from the device itself.  Integer status: 0 = success,
+ * otherwise a W2D_E* code with a message from w2d_last_error().
+ *
+ * Part 1 repeats the four exported functions of the reference engine
+ * (ll23002/DAS tsw_rtm/c_engine/wave2d.c) with identical signatures, so the
+ * reference's ctypes binding (tsw_rtm/wave_solver.py:19-71) can load this
+ * library in place of libwave2d.so.  They are synchronous and, like the
+ * reference, return nothing; failures are reported through w2d_last_error().
+ *
+ * Part 2 is the whole-loop engine that the Python layer (das_gb300.wave_solver,
+ * das_gb300.rtm_engine) drives: one call runs an entire forward propagation,
+ * backward propagation with imaging, or forward+backward migration of a shot,
+ * with every time step, injection, sampling and imaging on the device.
+ */
+#ifndef WAVE2D_CUDA_H
+#define WAVE2D_CUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define W2D_ABI_VERSION 1
+
+enum {
+    W2D_OK = 0,
+    W2D_EINVAL = 1,
+    W2D_ECUDA = 2,
+    W2D_ENOMEM = 3,
+    W2D_ETIMEOUT = 4,
+    W2D_EUNSUPPORTED = 5
+};
+
+/* ---- Part 1: reference-compatible per-step functions ------------------------ */
+
+/* Replaces acoustic_2d_step, wave2d.c:19-31.  One acoustic step; p_next's cells
+ * outside the updated interior keep their incoming values.  sponge may be NULL. */
+void acoustic_2d_step(const float* p_curr, const float* p_prev, float* p_next, const float* vel,
+                      const float* sponge, int nx, int nz, float dx, float dz, float dt,
+                      int free_surface_top);
+
+/* Replaces elastic_2d_step, wave2d.c:95-112.  Fields updated in place.  Where
+ * the reference reads row -1 (free surface on), this library reads zero. */
+void elastic_2d_step(float* vx, float* vz, float* sxx, float* szz, float* sxz,
+                     const float* lambda_, const float* mu, const float* buo_x,
+                     const float* buo_z, const float* sponge, int nx, int nz, float dx, float dz,
+                     float dt, int free_surface_top);
+
+/* Replaces correlate_imaging_condition, wave2d.c:218-225: image += src*rec*dt. */
+void correlate_imaging_condition(const float* src_wavefield, const float* rec_wavefield,
+                                 float* image, int nx, int nz, float dt);
+
+/* Replaces build_cerjan_sponge, wave2d.c:237-244 (host computation, host expf). */
+void build_cerjan_sponge(float* sponge, int nx, int nz, int n_sponge, float alpha,
+                         int free_surface_top);
+
+/* The same three operations with an int status (no counterpart in the reference,
+ * whose functions return void). */
+int w2d_acoustic_2d_step_status(const float* p_curr, const float* p_prev, float* p_next,
+                                const float* vel, const float* sponge, int nx, int nz, float dx,
+                                float dz, float dt, int free_surface_top);
+int w2d_elastic_2d_step_status(float* vx, float* vz, float* sxx, float* szz, float* sxz,
+                               const float* lambda_, const float* mu, const float* buo_x,
+                               const float* buo_z, const float* sponge, int nx, int nz, float dx,
+                               float dz, float dt, int free_surface_top);
+int w2d_correlate_status(const float* src, const float* rec, float* image, int nx, int nz,
+                         float dt);
+
+/* ---- Part 2: whole-loop engine ------------------------------------------------ */
+
+const char* w2d_last_error(void);
+int w2d_version(void);
+
+/* Sponge values by integer frame distance 0..n_sponge (lut[0] = 1). */
+int w2d_sponge_lut(float* lut, int n_sponge, float alpha);
+
+typedef struct w2d_engine w2d_engine;
+
+/* One propagation grid (WaveSolver2D.__init__, wave_solver.py:89-117).
+ * sponge: the (nz, nx) array the solver holds, or NULL for no sponge.  A sponge
+ * equal to the Cerjan table of some (n_sponge, alpha) is applied from a
+ * per-distance table; any other array is read per cell. */
+int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, float dt,
+                      const float* sponge, int free_surface_top);
+void w2d_engine_destroy(w2d_engine* e);
+
+/* Velocity model for slot 0 (forward / sediment flood) or 1 (backward / rock flood). */
+int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel);
+
+/* Kernel tile shape (warps per CTA, rows per warp); 0,0 restores the default. */
+int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp);
+
+/* forward_propagate_acoustic, wave_solver.py:128-186.  rec_out: (nt, n_rec);
+ * snaps_out: (ceil(nt/interval), nz, nx) or NULL.  Indices already in range. */
+int w2d_forward(w2d_engine* e, int vel_slot, const float* wavelet, int nt, int src_ix,
+                int src_iz, const int* rec_ix, int n_rec, int rec_iz, float* rec_out,
+                float* snaps_out, int snapshot_interval);
+
+/* backward_propagate_and_correlate, wave_solver.py:188-242.  data: (nt, n_rec);
+ * fwd_snaps: (n_snaps, nz, nx); image: (nz, nx), accumulated in place. */
+int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int nt,
+                           const int* rec_ix, int n_rec, int rec_iz, const float* fwd_snaps,
+                           int n_snaps, float* image, int snapshot_interval);
+
+/* Storage of the forward wavefield during migration. */
+enum { W2D_STORE_AUTO = 0, W2D_STORE_ALL = 1, W2D_STORE_CHECKPOINT = 2 };
+
+/* TSWRTMEngine.migrate_shot, rtm_engine.py:49-104, entirely on the device:
+ * forward in velocity slot 0 with illumination, backward in slot 1 with imaging.
+ * If image_out / illum_out are NULL the shot is added to the device stack
+ * instead (see w2d_stack_*).  storage picks full snapshot storage or
+ * checkpointed recomputation (AUTO: full storage when it fits the budget). */
+int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, int src_iz,
+                     const float* data, const int* rec_ix, int n_rec, int rec_iz,
+                     int snapshot_interval, int storage, float* image_out, float* illum_out);
+
+/* Device stack of migrated shots (rtm_engine.py:142-143). */
+int w2d_stack_reset(w2d_engine* e);
+int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out);
+
+/* Device-resident shot inputs: stage a shot's wavelet (nt) and data (nt, n_rec)
+ * into engine-owned device memory under an integer slot, then migrate it with
+ * no host-to-device traffic in the call (used for device-timed benchmarks and
+ * by callers that prefetch shots). */
+int w2d_shot_stage(w2d_engine* e, int slot, const float* wavelet, int nt, const float* data,
+                   int n_rec);
+int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const int* rec_ix,
+                       int n_rec, int rec_iz, int snapshot_interval, int storage,
+                       float* image_out, float* illum_out);
+
+/* CUDA-event timer on the engine's stream (device milliseconds between the calls). */
+int w2d_engine_timer_start(w2d_engine* e);
+int w2d_engine_timer_stop(w2d_engine* e, float* ms);
+
+/* Select the CUDA device used by engines created afterwards on this host thread. */
+int w2d_set_device(int device);
+/* PCI bus id ("0000:xx:00.0") of the current device, for per-GPU monitoring. */
+int w2d_device_pci_bus_id(char* buf, int len);
+
+/* Page-locked host memory for fast host<->device copies of shot inputs/outputs. */
+int w2d_host_alloc(void** out, unsigned long long bytes);
+void w2d_host_free(void* p);
+
+/* Bytes of device memory the engine may use for snapshots/checkpoints (0 = 80 %
+ * of free memory at the time of the call). */
+int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes);
+
+/* Statistics of the last whole-loop call: storage mode used (1 all, 2 checkpoint),
+ * number of step kernels launched, recomputed forward steps, device ms. */
+int w2d_engine_last_stats(w2d_engine* e, int* storage_used, long long* step_launches,
+                          long long* recomputed_steps, float* device_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WAVE2D_CUDA_H */
