@@ -43,7 +43,7 @@ _SIGS = {
     "w2d_version": (c_int, []),
     "w2d_sponge_lut": (c_int, [c_void_p, c_int, c_float]),
     "w2d_engine_create": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_float, c_float,
-                                  c_float, c_void_p, c_int]),
+                                  ctypes.c_double, c_void_p, c_int]),
     "w2d_engine_destroy": (None, [c_void_p]),
     "w2d_engine_set_velocity": (c_int, [c_void_p, c_int, c_void_p]),
     "w2d_engine_set_tile": (c_int, [c_void_p, c_int, c_int]),

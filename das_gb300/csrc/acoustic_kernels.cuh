@@ -282,11 +282,19 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
+template <int WARPS, int RPW>
+inline void launch_acoustic_step(const CUtensorMap& tm, const AcGeom& g, const AcStep& s,
+                                 cudaStream_t st)
+{
+    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + WARPS * RPW - 1) / (WARPS * RPW));
+    acoustic_step_kernel<WARPS, RPW><<<grid, WARPS * 32, 0, st>>>(tm, g, s);
+}
+
 // Injection into a field before the first step of a pass (forward: the source
 // sample w[0]; backward: receiver row nt-1).  One thread per column, receivers
 // of a column added in index order so repeated indices accumulate as the
 // reference's per-receiver Python loop does.
-__global__ void inject_kernel(float* p, AcGeom g, const float* w, const float* data_row,
+static __global__ void inject_kernel(float* p, AcGeom g, const float* w, const float* data_row,
                               float dt2_inj)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;

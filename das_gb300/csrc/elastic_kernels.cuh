@@ -42,7 +42,7 @@ __device__ __forceinline__ float el_dbwd(float am2, float am1, float a0, float a
     return fadd(fmul(k1, fsub(a0, am1)), fmul(k2, fsub(ap1, am2)));
 }
 
-__global__ void __launch_bounds__(256) elastic_velocity_kernel(ElGeom g, ElFields f)
+static __global__ void __launch_bounds__(256) elastic_velocity_kernel(ElGeom g, ElFields f)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     const int iz = blockIdx.y * blockDim.y + threadIdx.y;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) elastic_velocity_kernel(ElGeom g, ElField
     f.vz[c] = vz;
 }
 
-__global__ void __launch_bounds__(256) elastic_stress_kernel(ElGeom g, ElFields f)
+static __global__ void __launch_bounds__(256) elastic_stress_kernel(ElGeom g, ElFields f)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     const int iz = blockIdx.y * blockDim.y + threadIdx.y;

@@ -11,50 +11,13 @@
 #include <vector>
 
 #include "acoustic_kernels.cuh"
+#include "small_kernels.cuh"
 #include "w2d_common.cuh"
 #include "wave2d_cuda.h"
 
 namespace w2d {
 
 float cerjan_value(int d, float alpha);
-
-// ---- small elementwise kernels ------------------------------------------------
-__global__ void v2dt2_kernel(float* out, const float* vel, size_t n, float dt2)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const float v = vel[i];
-        out[i] = fmul(fmul(v, v), dt2);  // v * v * dt2 (wave2d.c:60-61)
-    }
-}
-
-__global__ void scale_kernel(float* a, size_t n, float s)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x)
-        a[i] = fmul(a[i], s);
-}
-
-__global__ void add_kernel(float* acc, const float* x, size_t n)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x)
-        acc[i] = fadd(acc[i], x[i]);
-}
-
-__global__ void correlate_kernel(const float* src, const float* rec, float* image, size_t n,
-                                 float dt)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x)
-        image[i] = fadd(image[i], fmul(fmul(src[i], rec[i]), dt));
-}
-
-static int grid_for(size_t n, int block = 256)
-{
-    size_t b = (n + block - 1) / block;
-    return (int)std::min<size_t>(b, 152 * 16);
-}
 
 // ---- tile-shape dispatch ------------------------------------------------------
 struct TileShape {
@@ -120,7 +83,8 @@ using namespace w2d;
 
 struct w2d_engine {
     int nx = 0, nz = 0, ldx = 0, fs = 1;
-    float dx = 0, dz = 0, dt = 0;
+    float dx = 0, dz = 0, dt = 0;  // dt as the float the reference C code receives
+    double dt_d = 0;               // dt as the Python float the reference drivers hold
     float inv_dx2 = 0, inv_dz2 = 0, dt2 = 0;
     size_t plane = 0;  // floats per pitched field
     cudaStream_t stream = nullptr;
@@ -241,7 +205,7 @@ AcStep base_step(w2d_engine* e, int slot)
     AcStep s;
     memset(&s, 0, sizeof s);
     s.v2dt2 = e->v2dt2.p + (size_t)slot * e->plane;
-    s.dt2_inj = (float)((double)e->dt * (double)e->dt);
+    s.dt2_inj = (float)(e->dt_d * e->dt_d);
     s.err = e->err.p;
     return s;
 }
@@ -379,7 +343,7 @@ size_t free_budget(w2d_engine* e)
 
 extern "C" {
 
-int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, float dt,
+int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, double dt,
                       const float* sponge, int free_surface_top)
 {
     W2D_CHECK_ARG(out, "out is NULL");
@@ -393,11 +357,12 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, floa
     e->plane = (size_t)e->ldx * nz;
     e->dx = dx;
     e->dz = dz;
-    e->dt = dt;
+    e->dt = (float)dt;
+    e->dt_d = dt;
     e->fs = free_surface_top ? 1 : 0;
     e->inv_dx2 = 1.0f / (dx * dx);
     e->inv_dz2 = 1.0f / (dz * dz);
-    e->dt2 = dt * dt;
+    e->dt2 = e->dt * e->dt;
     int rc = W2D_OK;
     auto fail = [&](int code) {
         w2d_engine_destroy(e);
@@ -565,7 +530,7 @@ int w2d_forward(w2d_engine* e, int vel_slot, const float* wavelet, int nt, int s
     e->last_launches = 0;
     e->last_recompute = 0;
     e->last_storage = 0;
-    const float dt2inj = (float)((double)e->dt * (double)e->dt);
+    const float dt2inj = (float)(e->dt_d * e->dt_d);
     cudaEventRecord(e->ev0, e->stream);
     if ((rc = forward_begin(e, dt2inj))) return rc;
     FwdOpts o;
@@ -626,8 +591,8 @@ int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int n
     e->cur_data = e->data.p;
     e->last_launches = 0;
     e->last_recompute = 0;
-    const float dt2inj = (float)((double)e->dt * (double)e->dt);
-    const float img_dt = (float)((double)e->dt * (double)snapshot_interval);
+    const float dt2inj = (float)(e->dt_d * e->dt_d);
+    const float img_dt = (float)(e->dt_d * (double)snapshot_interval);
     cudaEventRecord(e->ev0, e->stream);
     if (n_rec > 0) {
         if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
@@ -690,8 +655,8 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
     e->last_launches = 0;
     e->last_recompute = 0;
     e->last_storage = mode;
-    const float dt2inj = (float)((double)e->dt * (double)e->dt);
-    const float img_dt = (float)((double)e->dt * (double)interval);
+    const float dt2inj = (float)(e->dt_d * e->dt_d);
+    const float img_dt = (float)(e->dt_d * (double)interval);
     cudaEventRecord(e->ev0, e->stream);
     W2D_CUDA_TRY(cudaMemsetAsync(e->illum.p, 0, plane_b, e->stream));
     W2D_CUDA_TRY(cudaMemsetAsync(e->image.p, 0, plane_b, e->stream));
@@ -911,149 +876,6 @@ int w2d_engine_last_stats(w2d_engine* e, int* storage_used, long long* step_laun
     if (recomputed_steps) *recomputed_steps = e->last_recompute;
     if (device_ms) *device_ms = e->last_ms;
     return W2D_OK;
-}
-
-// ---- reference-compatible per-step entry points ------------------------------
-
-static std::mutex g_legacy_mu;
-static struct {
-    int nx = 0, nz = 0, ldx = 0;
-    DevBuf<float> buf;  // p_curr, p_prev, p_next, v2dt2, sponge, vel staging
-    DevBuf<int> shot, rec_ptr;
-    DevBuf<unsigned> err;
-    CUtensorMap tm;
-    cudaStream_t stream = nullptr;
-} g_leg;
-
-static int legacy_prepare(int nx, int nz)
-{
-    if (!g_leg.stream && cudaStreamCreateWithFlags(&g_leg.stream, cudaStreamNonBlocking)) {
-        set_error("stream creation failed");
-        return W2D_ECUDA;
-    }
-    const int ldx = pitch_for(nx);
-    const size_t plane = (size_t)ldx * nz;
-    int rc;
-    if ((rc = g_leg.shot.ensure(4)) || (rc = g_leg.err.ensure(1))) return rc;
-    if (g_leg.nx != nx || g_leg.nz != nz) {
-        if ((rc = g_leg.buf.ensure(6 * plane)) || (rc = g_leg.rec_ptr.ensure(nx + 1))) return rc;
-        W2D_CUDA_TRY(cudaMemset(g_leg.buf.p, 0, 6 * plane * 4));
-        W2D_CUDA_TRY(cudaMemset(g_leg.rec_ptr.p, 0, (nx + 1) * 4));
-        int sh[4] = {-1, -1, -1, 0};
-        W2D_CUDA_TRY(cudaMemcpy(g_leg.shot.p, sh, sizeof sh, cudaMemcpyHostToDevice));
-        W2D_CUDA_TRY(cudaMemset(g_leg.err.p, 0, 4));
-        if ((rc = make_tensor_map_2d(&g_leg.tm, g_leg.buf.p, nx, nz, ldx, AC_SW, 32 + 4))) return rc;
-        g_leg.nx = nx;
-        g_leg.nz = nz;
-        g_leg.ldx = ldx;
-    }
-    return W2D_OK;
-}
-
-static int legacy_acoustic(const float* p_curr, const float* p_prev, float* p_next,
-                           const float* vel, const float* sponge, int nx, int nz, float dx,
-                           float dz, float dt, int fs)
-{
-    W2D_CHECK_ARG(p_curr && p_prev && p_next && vel, "NULL field");
-    W2D_CHECK_ARG(nx >= 5 && nz >= 5, "grid must be at least 5 x 5");
-    std::lock_guard<std::mutex> lk(g_legacy_mu);
-    int rc;
-    if ((rc = legacy_prepare(nx, nz))) return rc;
-    const int ldx = g_leg.ldx;
-    const size_t plane = (size_t)ldx * nz;
-    float* d = g_leg.buf.p;
-    float *dc = d, *dp = d + plane, *dn = d + 2 * plane, *dv = d + 3 * plane, *ds = d + 4 * plane,
-          *dvel = d + 5 * plane;
-    cudaStream_t st = g_leg.stream;
-    const size_t hp = (size_t)nx * 4, dp_b = (size_t)ldx * 4;
-    W2D_CUDA_TRY(cudaMemcpy2DAsync(dc, dp_b, p_curr, hp, hp, nz, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpy2DAsync(dp, dp_b, p_prev, hp, hp, nz, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpy2DAsync(dn, dp_b, p_next, hp, hp, nz, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpy2DAsync(dvel, dp_b, vel, hp, hp, nz, cudaMemcpyHostToDevice, st));
-    if (sponge)
-        W2D_CUDA_TRY(cudaMemcpy2DAsync(ds, dp_b, sponge, hp, hp, nz, cudaMemcpyHostToDevice, st));
-    v2dt2_kernel<<<grid_for(plane), 256, 0, st>>>(dv, dvel, plane, dt * dt);
-    AcGeom g;
-    memset(&g, 0, sizeof g);
-    g.nx = nx;
-    g.nz = nz;
-    g.ldx = ldx;
-    g.inv_dx2 = 1.0f / (dx * dx);
-    g.inv_dz2 = 1.0f / (dz * dz);
-    g.free_surface = fs ? 1 : 0;
-    g.sponge_arr = sponge ? ds : nullptr;
-    g.rec_ptr = g_leg.rec_ptr.p;
-    g.rec_list = g_leg.rec_ptr.p;
-    g.shot = g_leg.shot.p;
-    AcStep s;
-    memset(&s, 0, sizeof s);
-    s.p_prev = dp;
-    s.p_next = dn;
-    s.v2dt2 = dv;
-    s.err = g_leg.err.p;
-    launch_t<8, 4>(g_leg.tm, g, s, st);
-    W2D_CUDA_TRY(cudaGetLastError());
-    W2D_CUDA_TRY(cudaMemcpy2DAsync(p_next, hp, dn, dp_b, hp, nz, cudaMemcpyDeviceToHost, st));
-    unsigned h = 0;
-    W2D_CUDA_TRY(cudaMemcpyAsync(&h, g_leg.err.p, 4, cudaMemcpyDeviceToHost, st));
-    W2D_CUDA_TRY(cudaStreamSynchronize(st));
-    if (h) {
-        cudaMemset(g_leg.err.p, 0, 4);
-        set_error("device wait gave up in acoustic_2d_step");
-        return W2D_ETIMEOUT;
-    }
-    return W2D_OK;
-}
-
-void acoustic_2d_step(const float* p_curr, const float* p_prev, float* p_next, const float* vel,
-                      const float* sponge, int nx, int nz, float dx, float dz, float dt,
-                      int free_surface_top)
-{
-    legacy_acoustic(p_curr, p_prev, p_next, vel, sponge, nx, nz, dx, dz, dt, free_surface_top);
-}
-
-int w2d_acoustic_2d_step_status(const float* p_curr, const float* p_prev, float* p_next,
-                                const float* vel, const float* sponge, int nx, int nz, float dx,
-                                float dz, float dt, int free_surface_top)
-{
-    return legacy_acoustic(p_curr, p_prev, p_next, vel, sponge, nx, nz, dx, dz, dt,
-                           free_surface_top);
-}
-
-static int legacy_correlate(const float* src, const float* rec, float* image, int nx, int nz,
-                            float dt)
-{
-    W2D_CHECK_ARG(src && rec && image && nx > 0 && nz > 0, "bad arguments");
-    std::lock_guard<std::mutex> lk(g_legacy_mu);
-    static DevBuf<float> buf;
-    static cudaStream_t st = nullptr;
-    if (!st && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) {
-        set_error("stream creation failed");
-        return W2D_ECUDA;
-    }
-    const size_t n = (size_t)nx * nz;
-    int rc;
-    if ((rc = buf.ensure(3 * n))) return rc;
-    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p, src, n * 4, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p + n, rec, n * 4, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(buf.p + 2 * n, image, n * 4, cudaMemcpyHostToDevice, st));
-    correlate_kernel<<<grid_for(n), 256, 0, st>>>(buf.p, buf.p + n, buf.p + 2 * n, n, dt);
-    W2D_CUDA_TRY(cudaGetLastError());
-    W2D_CUDA_TRY(cudaMemcpyAsync(image, buf.p + 2 * n, n * 4, cudaMemcpyDeviceToHost, st));
-    W2D_CUDA_TRY(cudaStreamSynchronize(st));
-    return W2D_OK;
-}
-
-void correlate_imaging_condition(const float* src_wavefield, const float* rec_wavefield,
-                                 float* image, int nx, int nz, float dt)
-{
-    legacy_correlate(src_wavefield, rec_wavefield, image, nx, nz, dt);
-}
-
-int w2d_correlate_status(const float* src, const float* rec, float* image, int nx, int nz,
-                         float dt)
-{
-    return legacy_correlate(src, rec, image, nx, nz, dt);
 }
 
 }  // extern "C"

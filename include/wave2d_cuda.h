@@ -84,7 +84,7 @@ typedef struct w2d_engine w2d_engine;
  * sponge: the (nz, nx) array the solver holds, or NULL for no sponge.  A sponge
  * equal to the Cerjan table of some (n_sponge, alpha) is applied from a
  * per-distance table; any other array is read per cell. */
-int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, float dt,
+int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, double dt,
                       const float* sponge, int free_surface_top);
 void w2d_engine_destroy(w2d_engine* e);
 

@@ -16,8 +16,19 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def golden():
+    """Golden arrays as a dict of materialised arrays.
+
+    Indexing an NpzFile decompresses a fresh array on every access; a raw
+    pointer (``.ctypes.data``) taken from such a temporary dangles as soon as
+    the temporary is collected, so tests get held arrays instead.
+    """
+    cache = {}
+
     def load(name):
-        return np.load(os.path.join(GOLDEN, f"golden_{name}.npz"))
+        if name not in cache:
+            with np.load(os.path.join(GOLDEN, f"golden_{name}.npz")) as z:
+                cache[name] = {k: z[k] for k in z.files}
+        return cache[name]
     return load
 
 

@@ -179,7 +179,7 @@ def main():
 
     # backward + imaging into a non-zero image (the image is accumulated in place)
     _, snaps_s = solver.forward_propagate_acoustic(vsmooth, w, 20, 2, rec_ix, 2, True, 3)
-    image0 = rng.standard_normal((nz, nx)).astype(np.float32) * 1e-12
+    image0 = rng.standard_normal((nz, nx)).astype(np.float32) * 1e-20
     image = image0.copy()
     solver.backward_propagate_and_correlate(vsmooth, rec, rec_ix, 2, snaps_s, image, 3)
     lp.update(bwd_image0=image0, bwd_image=image)

@@ -173,8 +173,10 @@ def test_migrate_multiple_golden(golden):
     res = eng.migrate_multiple_shots(fm, [g["wavelet"]] * 3, list(g["mm_src_ix"]), [2] * 3,
                                      list(g["mm_gathers"]), np.arange(s.nx), 2, 2)
     _close(res.raw_image, g["mm_raw"], IMG_TOL, what="raw")
-    _close(res.laplacian_image, g["mm_lap"], IMG_TOL, what="laplacian")
     _close(res.normalized_image, g["mm_norm"], IMG_TOL, what="normalized")
+    # scipy's convolve2d (the reference's Laplacian, also used here) rounds
+    # differently by an ulp between x86-64 and aarch64 builds: tolerance only
+    _close(res.laplacian_image, g["mm_lap"], IMG_TOL, exact=False, what="laplacian")
 
 
 # ---- engine vs live oracle over shapes, tiles and intervals ----------------------------
@@ -228,7 +230,7 @@ def test_f64_error_statement():
 
 
 def test_checkpoint_equals_full_storage_and_linearity():
-    """Recomputation is exact, and the image is linear in the data (scaling by 2 is exact)."""
+    """Recomputation is exact, and the image is linear in the data."""
     from das_gb300.rtm_engine import TSWRTMEngine
     from das_gb300.velocity_flood import FloodModels
     nz, nx = 120, 400
@@ -245,8 +247,10 @@ def test_checkpoint_equals_full_storage_and_linearity():
     assert s.last_stats()["recomputed_steps"] == len(w)
     np.testing.assert_array_equal(img_a, img_c)
     np.testing.assert_array_equal(ill_a, ill_c)
+    # linear in the data: doubling is exact in float32 except where a product falls
+    # into the subnormal range, which moves a rounding by an ulp here and there
     img_2, _ = TSWRTMEngine(s, "all").migrate_shot(fm, w, 200, 2, 2 * data, rix, 2, 2)
-    np.testing.assert_array_equal(img_2, 2 * img_a)
+    assert o.rel_l2(img_2, 2 * img_a) < 1e-6
 
 
 def test_errors_are_raised():
