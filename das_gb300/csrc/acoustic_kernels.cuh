@@ -97,54 +97,50 @@ struct AcTile {
     static constexpr unsigned TX_BYTES = SMEM_FLOATS * 4u;
 };
 
-template <int WARPS, int RPW>
-__global__ void __launch_bounds__(WARPS * 32)
-    acoustic_step_kernel(const __grid_constant__ CUtensorMap tm_curr, const AcGeom g, const AcStep s)
-{
-    static_assert(RPW >= 3, "free-surface rows 0..2 must belong to one warp");
-    using T = AcTile<WARPS, RPW>;
-    __shared__ __align__(128) float tile[T::SMEM_FLOATS];
-    __shared__ __align__(8) uint64_t bar;
+// Pointwise operands of one tile, loaded before the TMA box is waited for.
+template <int RPW>
+struct AcPoint {
+    float4 pp[RPW], vv[RPW], sp[RPW];
+};
 
+template <int WARPS, int RPW>
+__device__ __forceinline__ void ac_load_pointwise(const AcGeom& g, const AcStep& s, int x0, int z0,
+                                                  AcPoint<RPW>& P)
+{
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int x0 = blockIdx.x * AC_TX;
-    const int z0 = blockIdx.y * T::TZ;
-
-    if (threadIdx.x == 0) {
-        prefetch_tensormap(&tm_curr);
-        mbar_init(&bar, 1);
-        fence_mbar_init();
+    const int ixb = x0 + 4 * lane;
+    const int zr0 = z0 + warp * RPW;
+    const bool col_ok = ixb < g.ldx;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int iz = zr0 + r;
+        P.pp[r] = P.vv[r] = P.sp[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (col_ok && iz < g.nz) {
+            const size_t off = (size_t)iz * g.ldx + ixb;
+            P.pp[r] = __ldg(reinterpret_cast<const float4*>(s.p_prev + off));
+            P.vv[r] = __ldg(reinterpret_cast<const float4*>(s.v2dt2 + off));
+            if (g.sponge_arr) P.sp[r] = __ldg(reinterpret_cast<const float4*>(g.sponge_arr + off));
+        }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, T::TX_BYTES);
-        tma_load_2d(tile, &tm_curr, x0 - AC_HX, z0 - 2, &bar);
-    }
+}
 
+// Stencil, fused pointwise work and stores of one tile whose p_curr box (with
+// halo) is in shared memory.  Called by every thread of the CTA.
+template <int WARPS, int RPW>
+__device__ __forceinline__ void ac_tile_body(const float* tile, const AcGeom& g, const AcStep& s,
+                                             int x0, int z0, const AcPoint<RPW>& P)
+{
+    static_assert(RPW >= 3, "free-surface rows 0..2 must belong to one warp");
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int nx = g.nx, nz = g.nz, ldx = g.ldx;
     const int ixb = x0 + 4 * lane;
     const int zr0 = z0 + warp * RPW;
     const bool col_ok = ixb < ldx;
-
-    // pointwise operands, issued before waiting for the tile
-    float4 pp[RPW], vv[RPW], sp[RPW];
-#pragma unroll
-    for (int r = 0; r < RPW; ++r) {
-        const int iz = zr0 + r;
-        pp[r] = vv[r] = sp[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (col_ok && iz < nz) {
-            const size_t off = (size_t)iz * ldx + ixb;
-            pp[r] = __ldg(reinterpret_cast<const float4*>(s.p_prev + off));
-            vv[r] = __ldg(reinterpret_cast<const float4*>(s.v2dt2 + off));
-            if (g.sponge_arr) sp[r] = __ldg(reinterpret_cast<const float4*>(g.sponge_arr + off));
-        }
-    }
-
-    if (!mbar_wait_bounded(&bar, 0)) {
-        if (lane == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
-        return;
-    }
+    const float4* pp = P.pp;
+    const float4* vv = P.vv;
+    const float4* sp = P.sp;
 
     const int sc = AC_HX + 4 * lane;  // shared-memory column of this lane's first point
     const int sr0 = warp * RPW;       // shared-memory row of global row zr0 - 2
@@ -280,6 +276,34 @@ __global__ void __launch_bounds__(WARPS * 32)
             if (wr) row_next[ix] = val;
         }
     }
+}
+
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32)
+    acoustic_step_kernel(const __grid_constant__ CUtensorMap tm_curr, const AcGeom g, const AcStep s)
+{
+    using T = AcTile<WARPS, RPW>;
+    __shared__ __align__(128) float tile[T::SMEM_FLOATS];
+    __shared__ __align__(8) uint64_t bar;
+    const int x0 = blockIdx.x * AC_TX;
+    const int z0 = blockIdx.y * T::TZ;
+    if (threadIdx.x == 0) {
+        prefetch_tensormap(&tm_curr);
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, T::TX_BYTES);
+        tma_load_2d(tile, &tm_curr, x0 - AC_HX, z0 - 2, &bar);
+    }
+    AcPoint<RPW> P;
+    ac_load_pointwise<WARPS, RPW>(g, s, x0, z0, P);
+    if (!mbar_wait_bounded(&bar, 0)) {
+        if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    ac_tile_body<WARPS, RPW>(tile, g, s, x0, z0, P);
 }
 
 template <int WARPS, int RPW>
