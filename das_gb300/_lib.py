@@ -65,6 +65,18 @@ _SIGS = {
     "w2d_device_pci_bus_id": (c_int, [ctypes.c_char_p, c_int]),
     "w2d_host_alloc": (c_int, [ctypes.POINTER(c_void_p), c_ull]),
     "w2d_host_free": (None, [c_void_p]),
+    "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
+    "w2d_batch_destroy": (None, [c_void_p]),
+    "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    "w2d_batch_shot_bytes": (c_ull, [c_void_p]),
+    "w2d_batch_free_bytes": (c_ull, [c_void_p]),
+    "w2d_batch_submit": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
+    "w2d_batch_step": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
+    "w2d_batch_is_finished": (c_int, [c_void_p, c_int]),
+    "w2d_batch_fetch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
+    "w2d_batch_cancel": (c_int, [c_void_p, c_int]),
+    "w2d_batch_stats": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_float),
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_ll)]),
     "w2d_engine_last_stats": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_ll),
                                       ctypes.POINTER(c_ll), ctypes.POINTER(c_float)]),
 }

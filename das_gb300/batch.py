@@ -1,0 +1,180 @@
+"""Batched, continuously fed RTM on one GB300 (ctypes over the w2d_batch C ABI).
+
+The reference migrates shots one after another (tsw_rtm/rtm_engine.py:125-143).
+Here many shots -- each with its own grid size, length, models, wavelet and
+receivers -- are admitted into a device memory arena while memory allows and
+advanced together by one persistent kernel per launch over a (step, shot, tile)
+work queue; the time loop is a captured CUDA graph; finished shots leave and
+new ones enter between graph replays.  Each shot's result is bit-identical to
+migrating it alone with ``TSWRTMEngine.migrate_shot``: the arithmetic of every
+cell is the same fused step, independent of what else is in the batch.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from .geometry import normalize_index, normalize_indices
+
+
+class _ShotDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("dx", ctypes.c_float),
+                ("dz", ctypes.c_float), ("dt", ctypes.c_double), ("free_surface", ctypes.c_int),
+                ("n_sponge", ctypes.c_int), ("sponge_alpha", ctypes.c_float),
+                ("nt", ctypes.c_int), ("snapshot_interval", ctypes.c_int), ("n_rec", ctypes.c_int),
+                ("src_ix", ctypes.c_int), ("src_iz", ctypes.c_int), ("rec_iz", ctypes.c_int),
+                ("vel_fwd", ctypes.c_void_p), ("vel_bwd", ctypes.c_void_p),
+                ("wavelet", ctypes.c_void_p), ("data", ctypes.c_void_p),
+                ("rec_ix", ctypes.c_void_p)]
+
+
+@dataclass
+class ShotJob:
+    """One shot's migration: the arguments of WaveSolver2D + TSWRTMEngine.migrate_shot."""
+    nx: int
+    nz: int
+    dx: float
+    dz: float
+    dt: float
+    vel_fwd: np.ndarray
+    vel_bwd: np.ndarray
+    wavelet: np.ndarray
+    data: np.ndarray
+    receiver_ix: np.ndarray
+    source_ix: int
+    source_iz: int
+    receiver_iz: int = 2
+    snapshot_interval: int = 2
+    n_sponge: int = 30
+    sponge_alpha: float = 0.0015
+    free_surface_top: bool = True
+    tag: object = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    def desc(self) -> _ShotDesc:
+        vf = np.ascontiguousarray(self.vel_fwd, dtype=np.float32)
+        vb = np.ascontiguousarray(self.vel_bwd, dtype=np.float32)
+        w = np.ascontiguousarray(self.wavelet, dtype=np.float32).reshape(-1)
+        data = np.ascontiguousarray(self.data, dtype=np.float32)
+        if vf.shape != (self.nz, self.nx) or vb.shape != (self.nz, self.nx):
+            raise ValueError("velocity model shape does not match (nz, nx)")
+        if data.ndim != 2 or data.shape[0] != len(w):
+            raise ValueError("data must be (nt, n_receivers) with nt = len(wavelet)")
+        rix = normalize_indices(self.receiver_ix, self.nx, "receiver_ix")[: data.shape[1]]
+        if len(rix) < data.shape[1]:
+            raise IndexError("fewer receiver indices than data columns")
+        self._keep = [vf, vb, w, data, rix]
+        return _ShotDesc(self.nx, self.nz, self.dx, self.dz, self.dt,
+                         1 if self.free_surface_top else 0, int(self.n_sponge),
+                         float(self.sponge_alpha), len(w), int(self.snapshot_interval),
+                         data.shape[1], normalize_index(self.source_ix, self.nx, "source_ix"),
+                         normalize_index(self.source_iz, self.nz, "source_iz"),
+                         normalize_index(self.receiver_iz, self.nz, "receiver_iz"),
+                         vf.ctypes.data, vb.ctypes.data, w.ctypes.data,
+                         data.ctypes.data if data.size else None, rix.ctypes.data)
+
+    @property
+    def counted_points(self) -> int:
+        return 2 * self.nx * self.nz * len(self.wavelet)
+
+
+class BatchEngine:
+    """Persistent multi-shot RTM engine with admission by device-memory budget."""
+
+    def __init__(self, arena_bytes: int = 0, max_shots: int = 1024, tile=(8, 4),
+                 steps_per_launch: int = 16, launches_per_graph: int = 8):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.w2d_batch_create(ctypes.byref(h), int(arena_bytes), int(max_shots)))
+        self._h = h
+        self.config = None
+        self.set_config(tile, steps_per_launch, launches_per_graph)
+        self.last_ms = 0.0
+        self.last_points = 0.0
+
+    def set_config(self, tile, steps_per_launch, launches_per_graph):
+        _lib.check(self._lib.w2d_batch_set_config(self._h, int(tile[0]), int(tile[1]),
+                                                  int(steps_per_launch), int(launches_per_graph)))
+        self.config = (tuple(tile), int(steps_per_launch), int(launches_per_graph))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self._lib.w2d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def free_bytes(self) -> int:
+        return int(self._lib.w2d_batch_free_bytes(self._h))
+
+    @staticmethod
+    def shot_bytes(job: ShotJob) -> int:
+        """Device bytes a shot occupies while admitted (upper bound)."""
+        d = job.desc()
+        return int(_lib.load().w2d_batch_shot_bytes(ctypes.byref(d)))
+
+    def submit(self, job: ShotJob) -> Optional[int]:
+        """Admit a shot; None when it does not fit in device memory right now."""
+        d = job.desc()
+        slot = ctypes.c_int(-1)
+        rc = self._lib.w2d_batch_submit(self._h, ctypes.byref(d), ctypes.byref(slot))
+        if rc == 3:  # W2D_ENOMEM: wait for running shots to leave
+            return None
+        _lib.check(rc)
+        return slot.value
+
+    def step(self) -> int:
+        """Replay the captured time loop once; returns how many shots finished."""
+        n = ctypes.c_int(0)
+        _lib.check(self._lib.w2d_batch_step(self._h, ctypes.byref(n)))
+        na, ms, pts, la = ctypes.c_int(), ctypes.c_float(), ctypes.c_double(), ctypes.c_longlong()
+        _lib.check(self._lib.w2d_batch_stats(self._h, ctypes.byref(na), ctypes.byref(ms),
+                                             ctypes.byref(pts), ctypes.byref(la)))
+        self.last_ms, self.last_points, self.last_launches = ms.value, pts.value, la.value
+        self.n_active = na.value
+        return n.value
+
+    def finished(self, slot: int) -> bool:
+        return self._lib.w2d_batch_is_finished(self._h, int(slot)) == 1
+
+    def fetch(self, slot: int, nz: int, nx: int) -> Tuple[np.ndarray, np.ndarray]:
+        img = np.empty((nz, nx), np.float32)
+        ill = np.empty((nz, nx), np.float32)
+        _lib.check(self._lib.w2d_batch_fetch(self._h, int(slot), img.ctypes.data, ill.ctypes.data))
+        return img, ill
+
+    def run(self, jobs: Sequence[ShotJob]) -> Tuple[List[Tuple[np.ndarray, np.ndarray]], dict]:
+        """Migrate every job (continuous admission); results in job order and statistics."""
+        results: List[Optional[Tuple[np.ndarray, np.ndarray]]] = [None] * len(jobs)
+        pending = list(range(len(jobs)))
+        running: Dict[int, int] = {}
+        dev_ms = 0.0
+        pts = 0.0
+        launches = 0
+        max_active = 0
+        while pending or running:
+            while pending:
+                slot = self.submit(jobs[pending[0]])
+                if slot is None:
+                    break
+                running[slot] = pending.pop(0)
+            if not running:
+                raise MemoryError("a shot does not fit in the arena even when it is empty")
+            max_active = max(max_active, len(running))
+            self.step()
+            dev_ms += self.last_ms
+            pts += self.last_points
+            launches += self.last_launches
+            for slot in [s for s in running if self.finished(s)]:
+                j = running.pop(slot)
+                results[j] = self.fetch(slot, jobs[j].nz, jobs[j].nx)
+        return results, {"device_ms": dev_ms, "counted_points": pts, "launches": launches,
+                         "max_active": max_active}

@@ -1,10 +1,10 @@
 // acoustic_kernels.cuh -- fused 2D acoustic time-step kernels for sm_103a.
 //
-// One launch advances one wavefield by one step of the reference scheme
-// (tsw_rtm/c_engine/wave2d.c:19-82): 4th-order Laplacian in x and z,
-// second-order leapfrog, Cerjan sponge multiply on the interior, free-surface
-// rows 0 and 1 rewritten after the interior.  Everything else the reference
-// does around that call in Python (tsw_rtm/wave_solver.py:157-183 and
+// One tile-step advances a 128 (x) by TZ (z) tile of one wavefield by one step of
+// the reference scheme (tsw_rtm/c_engine/wave2d.c:19-82): 4th-order Laplacian in
+// x and z, second-order leapfrog, Cerjan sponge multiply on the interior,
+// free-surface rows 0 and 1 rewritten after the interior.  Everything else the
+// reference does around that call in Python (tsw_rtm/wave_solver.py:157-183 and
 // :210-242) is fused into the same pass so each wavefield is read once:
 //   * receiver sampling of p_next (forward, wave_solver.py:177),
 //   * source injection of the NEXT step into p_next (forward, :159),
@@ -13,23 +13,29 @@
 //   * illumination accumulation sum(p_curr^2) (rtm_engine.py:89),
 //   * zero-lag imaging image += fwd * p_curr * dt (wave2d.c:218-231 at :230-240).
 //
-// Tiling: a CTA owns a 128 (x) by WARPS*RPW (z) tile.  p_curr arrives through
-// one TMA 2D box load with a 2-row / 4-column halo into shared memory; each lane
-// owns four consecutive x points (float4) and each warp walks RPW rows keeping
-// a five-row register window along z; the x halo comes from the neighbouring
-// lanes through warp shuffles (shared memory only at the warp's two ends).
-// p_prev and the velocity term are streamed with float4 loads issued before
-// the TMA wait.
+// Data movement: three 2D TMA boxes per tile land in shared memory on one
+// mbarrier -- p_curr with a 2-row / 4-column halo (136 x (TZ+4); the 4-column
+// halo keeps the box's x start 16-byte aligned), p_prev and vel^2 dt^2 (128 x TZ
+// each), plus the sponge when it is a per-cell array.  No register holds an
+// operand while the copies are in flight.  Each lane owns four consecutive x
+// points (float4); each warp walks RPW rows keeping a five-row register window
+// along z; the x halo comes from the neighbouring lanes through warp shuffles
+// (shared memory only at the warp's two ends).  p_next leaves with float4
+// stores.
 //
-// Cells the reference never writes (ix < 2, ix >= nx-2, iz >= nz-2, and iz < 2
-// without a free surface) keep their value in the p_next buffer; sampling or
-// injecting there reads that stale value, exactly as the reference's 3-buffer
-// rotation does.
+// Tiles that touch no boundary row/column, no sponge cell, no source and no
+// receiver row take a straight path (stencil + float4 store per row).  Other
+// tiles take the general path: cells the reference never writes (ix < 2,
+// ix >= nx-2, iz >= nz-2, and iz < 2 without a free surface) keep their value
+// in the p_next buffer; sampling or injecting there reads that stale value,
+// exactly as the reference's 3-buffer rotation does.
 #pragma once
 
 #include "w2d_common.cuh"
 
 namespace w2d {
+
+enum SpongeMode { SPONGE_NONE = 0, SPONGE_LUT = 1, SPONGE_ARRAY = 2 };
 
 // Geometry and per-shot constants of one acoustic propagation.
 struct AcGeom {
@@ -37,8 +43,7 @@ struct AcGeom {
     float inv_dx2, inv_dz2;  // 1/(dx*dx), 1/(dz*dz) in float32, as the reference
     int free_surface;
     int n_sponge;
-    const float* sponge_lut;  // n_sponge+1 values by integer frame distance, or null
-    const float* sponge_arr;  // full pitched sponge array, or null (then LUT or none)
+    const float* sponge_lut;  // n_sponge+1 values by integer frame distance (LUT mode)
     const int* rec_ptr;       // CSR over columns: receivers of column ix are
     const int* rec_list;      //   rec_list[rec_ptr[ix] .. rec_ptr[ix+1])
     const int* shot;          // device ints {src_ix, src_iz, rec_iz}
@@ -46,9 +51,7 @@ struct AcGeom {
 
 // Per-launch pointers (all optional ones may be null).
 struct AcStep {
-    const float* p_prev;
     float* p_next;
-    const float* v2dt2;      // vel*vel*dt2 per cell (pitched)
     float* snap_out;         // forward: copy of p_curr
     float* illum;            // forward: += p_curr^2
     float* rec_out;          // forward: samples of p_next at the receivers, one row
@@ -61,9 +64,28 @@ struct AcStep {
     unsigned* err;
 };
 
+// The TMA descriptors of one tile-step.
+struct AcMaps {
+    CUtensorMap curr;    // p_curr, box AC_SW x (TZ+4)
+    CUtensorMap prev;    // p_prev, box AC_TX x TZ
+    CUtensorMap vel;     // vel^2 dt^2, box AC_TX x TZ
+    CUtensorMap sponge;  // per-cell sponge, box AC_TX x TZ (SPONGE_ARRAY only)
+};
+
 constexpr int AC_TX = 128;  // tile width in x (32 lanes x float4)
 constexpr int AC_HX = 4;    // x halo kept in shared memory (2 used; 4 keeps TMA x aligned)
 constexpr int AC_SW = AC_TX + 2 * AC_HX;
+
+template <int WARPS, int RPW, int SPONGE>
+struct AcTile {
+    static constexpr int TZ = WARPS * RPW;
+    static constexpr int C_FLOATS = (TZ + 4) * AC_SW;
+    static constexpr int P_FLOATS = TZ * AC_TX;
+    static constexpr int S_FLOATS = SPONGE == SPONGE_ARRAY ? TZ * AC_TX : 0;
+    static constexpr int FLOATS = C_FLOATS + 2 * P_FLOATS + S_FLOATS;
+    static constexpr unsigned TX_BYTES = FLOATS * 4u;
+    static constexpr size_t SMEM_BYTES = FLOATS * 4u + 128;  // + mbarrier slot
+};
 
 __device__ __forceinline__ float lap5(float m2, float m1, float c, float p1, float p2)
 {
@@ -89,71 +111,106 @@ __device__ __forceinline__ int sponge_dist(int ix, int iz, int nx, int nz, int n
     return d;
 }
 
-template <int WARPS, int RPW>
-struct AcTile {
-    static constexpr int TZ = WARPS * RPW;
-    static constexpr int SH = TZ + 4;
-    static constexpr int SMEM_FLOATS = SH * AC_SW;
-    static constexpr unsigned TX_BYTES = SMEM_FLOATS * 4u;
-};
-
-// Pointwise operands of one tile, loaded before the TMA box is waited for.
-template <int RPW>
-struct AcPoint {
-    float4 pp[RPW], vv[RPW], sp[RPW];
-};
-
-template <int WARPS, int RPW>
-__device__ __forceinline__ void ac_load_pointwise(const AcGeom& g, const AcStep& s, int x0, int z0,
-                                                  AcPoint<RPW>& P)
+// Issue the TMA boxes of a tile at (x0, z0) onto `bar` (one elected thread).
+template <int WARPS, int RPW, int SPONGE>
+__device__ __forceinline__ void ac_issue_loads(float* smem, const AcMaps* m, int x0, int z0,
+                                               uint64_t* bar)
 {
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const int ixb = x0 + 4 * lane;
-    const int zr0 = z0 + warp * RPW;
-    const bool col_ok = ixb < g.ldx;
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    mbar_expect_tx(bar, T::TX_BYTES);
+    tma_load_2d(smem, &m->curr, x0 - AC_HX, z0 - 2, bar);
+    tma_load_2d(smem + T::C_FLOATS, &m->prev, x0, z0, bar);
+    tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar);
+    if (SPONGE == SPONGE_ARRAY)
+        tma_load_2d(smem + T::C_FLOATS + 2 * T::P_FLOATS, &m->sponge, x0, z0, bar);
+}
+
+// True when no cell of the tile needs boundary, sponge, source or receiver work.
+template <int WARPS, int RPW, int SPONGE>
+__device__ __forceinline__ bool ac_tile_is_plain(const AcGeom& g, const AcStep& s, int x0, int z0)
+{
+    constexpr int TZ = WARPS * RPW;
+    const int x1 = x0 + AC_TX - 1, z1 = z0 + TZ - 1;
+    if (x0 < 2 || x1 >= g.nx - 2 || z0 < 2 || z1 >= g.nz - 2) return false;
+    if (SPONGE == SPONGE_LUT) {
+        const int n = g.n_sponge;
+        if (x0 < n || x1 > g.nx - 1 - n || z1 > g.nz - 1 - n || (!g.free_surface && z0 < n))
+            return false;
+    }
+    if (s.inj_w || s.rec_out || s.inj_data) {
+        const int src_iz = g.shot[1], rec_iz = g.shot[2];
+        if (s.inj_w && src_iz >= z0 && src_iz <= z1) return false;
+        if ((s.rec_out || s.inj_data) && rec_iz >= z0 && rec_iz <= z1) return false;
+    }
+    return true;
+}
+
+// Stencil of one row of four points: reference operation order, no contraction.
+__device__ __forceinline__ void ac_row(const float e[8], const float4& w0, const float4& w1,
+                                       const float4& w3, const float4& w4, const float4& pp,
+                                       const float4& vv, float inv_dx2, float inv_dz2,
+                                       float u[4])
+{
 #pragma unroll
-    for (int r = 0; r < RPW; ++r) {
-        const int iz = zr0 + r;
-        P.pp[r] = P.vv[r] = P.sp[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (col_ok && iz < g.nz) {
-            const size_t off = (size_t)iz * g.ldx + ixb;
-            P.pp[r] = __ldg(reinterpret_cast<const float4*>(s.p_prev + off));
-            P.vv[r] = __ldg(reinterpret_cast<const float4*>(s.v2dt2 + off));
-            if (g.sponge_arr) P.sp[r] = __ldg(reinterpret_cast<const float4*>(g.sponge_arr + off));
-        }
+    for (int j = 0; j < 4; ++j) {
+        const float c = e[j + 2];
+        const float lx = fmul(lap5(e[j], e[j + 1], c, e[j + 3], e[j + 4]), inv_dx2);
+        const float lz = fmul(lap5(comp(w0, j), comp(w1, j), c, comp(w3, j), comp(w4, j)), inv_dz2);
+        u[j] = fadd(fsub(fmul(2.0f, c), comp(pp, j)), fmul(comp(vv, j), fadd(lx, lz)));
     }
 }
 
-// Stencil, fused pointwise work and stores of one tile whose p_curr box (with
-// halo) is in shared memory.  Called by every thread of the CTA.
-template <int WARPS, int RPW>
-__device__ __forceinline__ void ac_tile_body(const float* tile, const AcGeom& g, const AcStep& s,
-                                             int x0, int z0, const AcPoint<RPW>& P)
+// Snapshot / illumination / imaging of one row of p_curr (fused pointwise work).
+__device__ __forceinline__ void ac_fused_row(const AcStep& s, size_t off, const float4& c)
+{
+    if (s.snap_out) __stcs(reinterpret_cast<float4*>(s.snap_out + off), c);
+    if (s.illum) {
+        float4 a = *reinterpret_cast<float4*>(s.illum + off);
+        a.x = fadd(a.x, fmul(c.x, c.x));
+        a.y = fadd(a.y, fmul(c.y, c.y));
+        a.z = fadd(a.z, fmul(c.z, c.z));
+        a.w = fadd(a.w, fmul(c.w, c.w));
+        *reinterpret_cast<float4*>(s.illum + off) = a;
+    }
+    if (s.image) {
+        const float4 f = __ldcs(reinterpret_cast<const float4*>(s.snap_in + off));
+        float4 a = *reinterpret_cast<float4*>(s.image + off);
+        a.x = fadd(a.x, fmul(fmul(f.x, c.x), s.img_dt));
+        a.y = fadd(a.y, fmul(fmul(f.y, c.y), s.img_dt));
+        a.z = fadd(a.z, fmul(fmul(f.z, c.z), s.img_dt));
+        a.w = fadd(a.w, fmul(fmul(f.w, c.w), s.img_dt));
+        *reinterpret_cast<float4*>(s.image + off) = a;
+    }
+}
+
+// Stencil, fused pointwise work and stores of one tile whose boxes are in shared
+// memory.  Called by every thread of the CTA.
+template <int WARPS, int RPW, int SPONGE>
+__device__ __forceinline__ void ac_tile_body(const float* smem, const AcGeom& g, const AcStep& s,
+                                             int x0, int z0)
 {
     static_assert(RPW >= 3, "free-surface rows 0..2 must belong to one warp");
+    using T = AcTile<WARPS, RPW, SPONGE>;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nx = g.nx, nz = g.nz, ldx = g.ldx;
     const int ixb = x0 + 4 * lane;
     const int zr0 = z0 + warp * RPW;
     const bool col_ok = ixb < ldx;
-    const float4* pp = P.pp;
-    const float4* vv = P.vv;
-    const float4* sp = P.sp;
+    const float* tile = smem;
+    const float* tp = smem + T::C_FLOATS;
+    const float* tv = tp + T::P_FLOATS;
+    const float* ts = tv + T::P_FLOATS;
 
     const int sc = AC_HX + 4 * lane;  // shared-memory column of this lane's first point
     const int sr0 = warp * RPW;       // shared-memory row of global row zr0 - 2
     auto lds4 = [&](int srow) {
         return *reinterpret_cast<const float4*>(&tile[srow * AC_SW + sc]);
     };
-
-    float out[RPW][4];
-    float4 w0 = lds4(sr0 + 0), w1 = lds4(sr0 + 1), w2 = lds4(sr0 + 2), w3 = lds4(sr0 + 3);
-#pragma unroll
-    for (int r = 0; r < RPW; ++r) {
-        const float4 w4 = lds4(sr0 + r + 4);
-        const int srow = sr0 + r + 2;
+    auto pw4 = [&](const float* base, int r) {
+        return *reinterpret_cast<const float4*>(&base[(sr0 + r) * AC_TX + 4 * lane]);
+    };
+    auto x_halo = [&](const float4& w2, int srow, float e[8]) {
         float l2 = __shfl_up_sync(0xffffffffu, w2.z, 1);
         float l1 = __shfl_up_sync(0xffffffffu, w2.w, 1);
         float r1 = __shfl_down_sync(0xffffffffu, w2.x, 1);
@@ -166,59 +223,84 @@ __device__ __forceinline__ void ac_tile_body(const float* tile, const AcGeom& g,
             r1 = tile[srow * AC_SW + AC_HX + AC_TX];
             r2 = tile[srow * AC_SW + AC_HX + AC_TX + 1];
         }
-        const float e[8] = {l2, l1, w2.x, w2.y, w2.z, w2.w, r1, r2};
-        const int iz = zr0 + r;
+        e[0] = l2;
+        e[1] = l1;
+        e[2] = w2.x;
+        e[3] = w2.y;
+        e[4] = w2.z;
+        e[5] = w2.w;
+        e[6] = r1;
+        e[7] = r2;
+    };
+    const bool fused = s.snap_out || s.illum || s.image;
+
+    if (ac_tile_is_plain<WARPS, RPW, SPONGE>(g, s, x0, z0)) {
+        // ---- straight path: every cell of the tile is an interior cell ----
+        float4 w0 = lds4(sr0 + 0), w1 = lds4(sr0 + 1), w2 = lds4(sr0 + 2), w3 = lds4(sr0 + 3);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float c = e[j + 2];
-            const float lx = fmul(lap5(e[j], e[j + 1], c, e[j + 3], e[j + 4]), g.inv_dx2);
-            const float lz = fmul(lap5(comp(w0, j), comp(w1, j), c, comp(w3, j), comp(w4, j)),
-                                  g.inv_dz2);
-            float u = fadd(fsub(fmul(2.0f, c), comp(pp[r], j)), fmul(comp(vv[r], j), fadd(lx, lz)));
-            if (g.sponge_arr) {
-                u = fmul(u, comp(sp[r], j));
-            } else if (g.sponge_lut) {
-                const int d = sponge_dist(ixb + j, iz, nx, nz, g.n_sponge, g.free_surface);
-                if (d > 0) u = fmul(u, __ldg(g.sponge_lut + d));
+        for (int r = 0; r < RPW; ++r) {
+            const float4 w4 = lds4(sr0 + r + 4);
+            float e[8];
+            x_halo(w2, sr0 + r + 2, e);
+            float u[4];
+            ac_row(e, w0, w1, w3, w4, pw4(tp, r), pw4(tv, r), g.inv_dx2, g.inv_dz2, u);
+            if (SPONGE == SPONGE_ARRAY) {
+                const float4 sp = pw4(ts, r);
+                u[0] = fmul(u[0], sp.x);
+                u[1] = fmul(u[1], sp.y);
+                u[2] = fmul(u[2], sp.z);
+                u[3] = fmul(u[3], sp.w);
             }
-            out[r][j] = u;
+            const size_t off = (size_t)(zr0 + r) * ldx + ixb;
+            *reinterpret_cast<float4*>(s.p_next + off) = make_float4(u[0], u[1], u[2], u[3]);
+            if (fused) ac_fused_row(s, off, w2);
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = w4;
         }
-        w0 = w1;
-        w1 = w2;
-        w2 = w3;
-        w3 = w4;
+        return;
     }
 
-    // ---- fused pointwise work on p_curr (snapshot / illumination / imaging) ----
-    if (s.snap_out || s.illum || s.image) {
+    // ---- general path ----
+    float out[RPW][4];
+    {
+        float4 w0 = lds4(sr0 + 0), w1 = lds4(sr0 + 1), w2 = lds4(sr0 + 2), w3 = lds4(sr0 + 3);
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) {
+            const float4 w4 = lds4(sr0 + r + 4);
+            float e[8];
+            x_halo(w2, sr0 + r + 2, e);
+            float u[4];
+            ac_row(e, w0, w1, w3, w4, pw4(tp, r), pw4(tv, r), g.inv_dx2, g.inv_dz2, u);
+            const int iz = zr0 + r;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (SPONGE == SPONGE_ARRAY) {
+                    u[j] = fmul(u[j], comp(pw4(ts, r), j));
+                } else if (SPONGE == SPONGE_LUT) {
+                    const int d = sponge_dist(ixb + j, iz, nx, nz, g.n_sponge, g.free_surface);
+                    if (d > 0) u[j] = fmul(u[j], __ldg(g.sponge_lut + d));
+                }
+                out[r][j] = u[j];
+            }
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = w4;
+        }
+    }
+
+    if (fused) {
 #pragma unroll
         for (int r = 0; r < RPW; ++r) {
             const int iz = zr0 + r;
             if (!col_ok || iz >= nz) continue;
-            const float4 c = lds4(sr0 + r + 2);
-            const size_t off = (size_t)iz * ldx + ixb;
-            if (s.snap_out) __stcs(reinterpret_cast<float4*>(s.snap_out + off), c);
-            if (s.illum) {
-                float4 a = *reinterpret_cast<float4*>(s.illum + off);
-                a.x = fadd(a.x, fmul(c.x, c.x));
-                a.y = fadd(a.y, fmul(c.y, c.y));
-                a.z = fadd(a.z, fmul(c.z, c.z));
-                a.w = fadd(a.w, fmul(c.w, c.w));
-                *reinterpret_cast<float4*>(s.illum + off) = a;
-            }
-            if (s.image) {
-                const float4 f = __ldcs(reinterpret_cast<const float4*>(s.snap_in + off));
-                float4 a = *reinterpret_cast<float4*>(s.image + off);
-                a.x = fadd(a.x, fmul(fmul(f.x, c.x), s.img_dt));
-                a.y = fadd(a.y, fmul(fmul(f.y, c.y), s.img_dt));
-                a.z = fadd(a.z, fmul(fmul(f.z, c.z), s.img_dt));
-                a.w = fadd(a.w, fmul(fmul(f.w, c.w), s.img_dt));
-                *reinterpret_cast<float4*>(s.image + off) = a;
-            }
+            ac_fused_row(s, (size_t)iz * ldx + ixb, lds4(sr0 + r + 2));
         }
     }
 
-    // ---- stores, boundary rows, receivers and next-step injection ----
+    // stores, boundary rows, receivers and next-step injection
     const int src_ix = g.shot[0], src_iz = g.shot[1], rec_iz = g.shot[2];
     const bool rec_active = (s.rec_out != nullptr) || (s.inj_data != nullptr);
 #pragma unroll
@@ -278,40 +360,59 @@ __device__ __forceinline__ void ac_tile_body(const float* tile, const AcGeom& g,
     }
 }
 
-template <int WARPS, int RPW>
+// One tile per CTA, one launch per time step.
+template <int WARPS, int RPW, int SPONGE>
 __global__ void __launch_bounds__(WARPS * 32)
-    acoustic_step_kernel(const __grid_constant__ CUtensorMap tm_curr, const AcGeom g, const AcStep s)
+    acoustic_step_kernel(const __grid_constant__ AcMaps maps, const AcGeom g, const AcStep s)
 {
-    using T = AcTile<WARPS, RPW>;
-    __shared__ __align__(128) float tile[T::SMEM_FLOATS];
-    __shared__ __align__(8) uint64_t bar;
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    extern __shared__ __align__(128) float smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
     const int x0 = blockIdx.x * AC_TX;
     const int z0 = blockIdx.y * T::TZ;
     if (threadIdx.x == 0) {
-        prefetch_tensormap(&tm_curr);
-        mbar_init(&bar, 1);
+        prefetch_tensormap(&maps.curr);
+        mbar_init(bar, 1);
         fence_mbar_init();
+        ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, T::TX_BYTES);
-        tma_load_2d(tile, &tm_curr, x0 - AC_HX, z0 - 2, &bar);
-    }
-    AcPoint<RPW> P;
-    ac_load_pointwise<WARPS, RPW>(g, s, x0, z0, P);
-    if (!mbar_wait_bounded(&bar, 0)) {
+    if (!mbar_wait_bounded(bar, 0)) {
         if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
         return;
     }
-    ac_tile_body<WARPS, RPW>(tile, g, s, x0, z0, P);
+    ac_tile_body<WARPS, RPW, SPONGE>(smem, g, s, x0, z0);
 }
 
-template <int WARPS, int RPW>
-inline void launch_acoustic_step(const CUtensorMap& tm, const AcGeom& g, const AcStep& s,
-                                 cudaStream_t st)
+template <int WARPS, int RPW, int SPONGE>
+inline cudaError_t launch_acoustic_step(const AcMaps& m, const AcGeom& g, const AcStep& s,
+                                        cudaStream_t st)
 {
-    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + WARPS * RPW - 1) / (WARPS * RPW));
-    acoustic_step_kernel<WARPS, RPW><<<grid, WARPS * 32, 0, st>>>(tm, g, s);
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    static bool attr_set = false;  // one attribute call per instantiation
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(acoustic_step_kernel<WARPS, RPW, SPONGE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)T::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
+    acoustic_step_kernel<WARPS, RPW, SPONGE><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
+    return cudaGetLastError();
+}
+
+// Encode the TMA descriptors of one tile-step over pitched fields.
+inline int make_ac_maps(AcMaps* m, const float* curr, const float* prev, const float* vel,
+                        const float* sponge, int nx, int nz, int ldx, int tz)
+{
+    int rc;
+    if ((rc = make_tensor_map_2d(&m->curr, curr, nx, nz, ldx, AC_SW, tz + 4))) return rc;
+    if ((rc = make_tensor_map_2d(&m->prev, prev, nx, nz, ldx, AC_TX, tz))) return rc;
+    if ((rc = make_tensor_map_2d(&m->vel, vel, nx, nz, ldx, AC_TX, tz))) return rc;
+    if (sponge && (rc = make_tensor_map_2d(&m->sponge, sponge, nx, nz, ldx, AC_TX, tz))) return rc;
+    if (!sponge) m->sponge = m->vel;
+    return W2D_OK;
 }
 
 // Injection into a field before the first step of a pass (forward: the source
@@ -319,7 +420,7 @@ inline void launch_acoustic_step(const CUtensorMap& tm, const AcGeom& g, const A
 // of a column added in index order so repeated indices accumulate as the
 // reference's per-receiver Python loop does.
 static __global__ void inject_kernel(float* p, AcGeom g, const float* w, const float* data_row,
-                              float dt2_inj)
+                                     float dt2_inj)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     if (ix >= g.nx) return;

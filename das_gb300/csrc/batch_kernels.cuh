@@ -1,0 +1,199 @@
+// batch_kernels.cuh -- persistent multi-shot RTM kernel over a (step, shot, tile)
+// work queue.
+//
+// Many shots of different grid sizes and lengths advance together.  One launch
+// (a "chunk") covers S consecutive phase steps of every active shot; a shot's
+// phase step k is forward step k for k < nt and backward step 2*nt-1-k after
+// that, so a shot runs its whole forward-then-backward migration as one sequence
+// of 2*nt tile-steps.  Work items are numbered step-major (local step j, then
+// shot, then tile) and handed out with one atomic counter; a CTA processes an
+// item as soon as the 3 x 3 neighbouring tiles of the same shot have completed
+// phase step k-1 (per-tile counters with release/acquire), so steps overlap
+// across the grid instead of meeting at a kernel boundary.  Because items are
+// taken in increasing order, every item an item waits for was taken earlier by
+// a running CTA: the waits cannot deadlock.  Every wait is bounded; on timeout
+// the CTA raises an error bit that makes all CTAs stop.
+//
+// Why the dependency suffices: the plane written at step k (p_next) was p_prev
+// at step k-1 (read only by the same tile) and p_curr at step k-2 (read by the
+// tile and its neighbours through the halo); all of those reads belong to items
+// the 3 x 3 neighbourhood completed before it finished step k-1.
+#pragma once
+
+#include "acoustic_kernels.cuh"
+
+namespace w2d {
+
+// Device-resident descriptor of one shot of a batch.
+struct BShot {
+    AcGeom g;           // g.shot points at shot_ints of this descriptor
+    int shot_ints[4];   // src_ix, src_iz, rec_iz, n_rec
+    int nt, interval, n_rec;
+    int tiles_x, tiles_z, ntiles;
+    int k_end;          // 2 * nt phase steps
+    int k0;             // phase step at which the current chunk starts
+    int maps_index;     // index into the BMaps table
+    int pad_;
+    float* wave[6];     // forward triple, backward triple
+    float* snaps;       // ceil(nt/interval) snapshot planes
+    float* illum;
+    float* image;
+    const float* wavelet;
+    const float* data;
+    float dt2_inj, img_dt;
+    unsigned* done;     // per tile: phase steps completed
+};
+
+// TMA descriptors of one shot (global memory, 64-byte aligned).
+struct alignas(64) BMaps {
+    CUtensorMap curr[6];
+    CUtensorMap prev[6];
+    CUtensorMap vel[2];
+};
+
+struct BatchArgs {
+    BShot* shots;
+    const BMaps* maps;
+    const int* active;       // indices of active shots
+    const int* tile_prefix;  // prefix sums of their tile counts (n_active + 1)
+    const int* n_active;     // device scalar
+    int S;                   // phase steps per launch
+    unsigned* head;          // work counter (zeroed before each launch)
+    unsigned* err;
+};
+
+__device__ __forceinline__ bool wait_counter(const unsigned* p, unsigned target, unsigned* err)
+{
+    for (unsigned i = 0; i < (1u << 24); ++i) {
+        if (ld_acquire_u32(p) >= target) return true;
+        if (i > 64) __nanosleep(128);
+        if ((i & 1023) == 1023 && (*reinterpret_cast<volatile unsigned*>(err) & ERR_ABORT))
+            return false;
+    }
+    atomicOr(err, ERR_DEP_TIMEOUT | ERR_ABORT);
+    return false;
+}
+
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32) acoustic_batch_kernel(const BatchArgs a)
+{
+    using T = AcTile<WARPS, RPW, SPONGE_LUT>;
+    extern __shared__ __align__(128) float smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
+    __shared__ int s_item;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const int n_act = *a.n_active;
+    if (n_act <= 0) return;
+    const int T_all = a.tile_prefix[n_act];
+    const long long total = (long long)a.S * T_all;
+    unsigned phase = 0;
+    for (;;) {
+        if (tid == 0) {
+            s_item = (int)atomicAdd(a.head, 1u);
+            s_ok = (*reinterpret_cast<volatile unsigned*>(a.err) & ERR_ABORT) ? 0 : 1;
+        }
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= total || !s_ok) break;
+        const int j = (int)(item / T_all);
+        const int r = (int)(item - (long long)j * T_all);
+        int lo = 0, hi = n_act - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(a.tile_prefix + mid) <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        BShot* sh = a.shots + __ldg(a.active + lo);
+        const int t = r - __ldg(a.tile_prefix + lo);
+        const int k = sh->k0 + j;
+        if (k >= sh->k_end) {
+            __syncthreads();
+            continue;
+        }
+        const int tiles_x = sh->tiles_x, tiles_z = sh->tiles_z;
+        const int tx = t % tiles_x, tz = t / tiles_x;
+        if (tid < 9 && k > 0) {
+            const int nx_ = tx + tid % 3 - 1, nz_ = tz + tid / 3 - 1;
+            if (nx_ >= 0 && nx_ < tiles_x && nz_ >= 0 && nz_ < tiles_z)
+                if (!wait_counter(sh->done + nz_ * tiles_x + nx_, (unsigned)k, a.err)) s_ok = 0;
+        }
+        __syncthreads();
+        if (!s_ok) break;
+
+        // the tile-step of phase step k
+        const int nt = sh->nt, interval = sh->interval;
+        const BMaps* mp = a.maps + sh->maps_index;
+        AcStep s;
+        s.snap_out = nullptr;
+        s.illum = nullptr;
+        s.rec_out = nullptr;
+        s.snap_in = nullptr;
+        s.image = nullptr;
+        s.img_dt = sh->img_dt;
+        s.inj_w = nullptr;
+        s.inj_data = nullptr;
+        s.dt2_inj = sh->dt2_inj;
+        s.err = a.err;
+        int ci, pi, vi;
+        if (k < nt) {
+            const int it = k;
+            pi = it % 3;
+            ci = (it + 1) % 3;
+            s.p_next = sh->wave[(it + 2) % 3];
+            vi = 0;
+            if (it + 1 < nt) s.inj_w = sh->wavelet + it + 1;
+            if (it % interval == 0) {
+                s.snap_out = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
+                s.illum = sh->illum;
+            }
+        } else {
+            const int m = k - nt, it = nt - 1 - m;
+            pi = 3 + m % 3;
+            ci = 3 + (m + 1) % 3;
+            s.p_next = sh->wave[3 + (m + 2) % 3];
+            vi = 1;
+            if (it >= 1 && sh->n_rec > 0) s.inj_data = sh->data + (size_t)(it - 1) * sh->n_rec;
+            if (it % interval == 0) {
+                s.snap_in = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
+                s.image = sh->image;
+            }
+        }
+        const int x0 = tx * AC_TX, z0 = tz * T::TZ;
+        if (tid == 0) {
+            fence_proxy_async_global();
+            fence_proxy_async_shared();
+            mbar_expect_tx(bar, T::TX_BYTES);
+            tma_load_2d(smem, &mp->curr[ci], x0 - AC_HX, z0 - 2, bar);
+            tma_load_2d(smem + T::C_FLOATS, &mp->prev[pi], x0, z0, bar);
+            tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &mp->vel[vi], x0, z0, bar);
+        }
+        const bool got = mbar_wait_bounded(bar, phase);
+        if (__syncthreads_or(!got)) {
+            if (tid == 0) atomicOr(a.err, ERR_TMA_TIMEOUT | ERR_ABORT);
+            break;
+        }
+        phase ^= 1u;
+        ac_tile_body<WARPS, RPW, SPONGE_LUT>(smem, sh->g, s, x0, z0);
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_release_u32(sh->done + t, (unsigned)(k + 1));
+        }
+    }
+}
+
+// After each chunk: every active shot moves S phase steps on.
+static __global__ void batch_advance_kernel(BShot* shots, const int* active, const int* n_active,
+                                            int S)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *n_active) shots[active[i]].k0 += S;
+}
+
+}  // namespace w2d

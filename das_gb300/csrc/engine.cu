@@ -28,24 +28,25 @@ struct TileShape {
 static bool tile_supported(int warps, int rpw)
 {
     return (warps == 8 && rpw == 4) || (warps == 4 && rpw == 8) || (warps == 8 && rpw == 8) ||
-           (warps == 4 && rpw == 4) || (warps == 16 && rpw == 4);
+           (warps == 4 && rpw == 4);
 }
 
 template <int W, int R>
-static void launch_t(const CUtensorMap& tm, const AcGeom& g, const AcStep& s, cudaStream_t st)
+static cudaError_t launch_sp(int sponge_mode, const AcMaps& m, const AcGeom& g, const AcStep& s,
+                             cudaStream_t st)
 {
-    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + W * R - 1) / (W * R));
-    acoustic_step_kernel<W, R><<<grid, W * 32, 0, st>>>(tm, g, s);
+    if (sponge_mode == SPONGE_LUT) return launch_acoustic_step<W, R, SPONGE_LUT>(m, g, s, st);
+    if (sponge_mode == SPONGE_ARRAY) return launch_acoustic_step<W, R, SPONGE_ARRAY>(m, g, s, st);
+    return launch_acoustic_step<W, R, SPONGE_NONE>(m, g, s, st);
 }
 
-static void launch_step(TileShape t, const CUtensorMap& tm, const AcGeom& g, const AcStep& s,
-                        cudaStream_t st)
+static cudaError_t launch_step(TileShape t, int sponge_mode, const AcMaps& m, const AcGeom& g,
+                               const AcStep& s, cudaStream_t st)
 {
-    if (t.warps == 8 && t.rpw == 4) launch_t<8, 4>(tm, g, s, st);
-    else if (t.warps == 4 && t.rpw == 8) launch_t<4, 8>(tm, g, s, st);
-    else if (t.warps == 8 && t.rpw == 8) launch_t<8, 8>(tm, g, s, st);
-    else if (t.warps == 4 && t.rpw == 4) launch_t<4, 4>(tm, g, s, st);
-    else launch_t<16, 4>(tm, g, s, st);
+    if (t.warps == 4 && t.rpw == 8) return launch_sp<4, 8>(sponge_mode, m, g, s, st);
+    if (t.warps == 8 && t.rpw == 8) return launch_sp<8, 8>(sponge_mode, m, g, s, st);
+    if (t.warps == 4 && t.rpw == 4) return launch_sp<4, 4>(sponge_mode, m, g, s, st);
+    return launch_sp<8, 4>(sponge_mode, m, g, s, st);
 }
 
 // ---- device buffer helper -------------------------------------------------------
@@ -96,7 +97,9 @@ struct w2d_engine {
     bool use_lut = false, use_arr = false;
 
     DevBuf<float> waves;  // 6 planes: forward triple then backward triple
-    CUtensorMap tm[6];
+    // TMA descriptors for the current tile height: each wave plane as p_curr (halo
+    // box) and as p_prev, each v^2 dt^2 slot, and the per-cell sponge
+    CUtensorMap map_curr[6], map_prev[6], map_vel[2], map_sponge;
     int tm_tz = -1;
     DevBuf<float> v2dt2;  // 2 planes (slot 0 forward model, slot 1 backward model)
     bool vel_set[2] = {false, false};
@@ -145,11 +148,40 @@ int ensure_tensor_maps(w2d_engine* e)
 {
     const int tz = e->tile.tz();
     if (e->tm_tz == tz) return W2D_OK;
+    int rc;
     for (int i = 0; i < 6; ++i) {
-        int rc = make_tensor_map_2d(&e->tm[i], e->wave(i), e->nx, e->nz, e->ldx, AC_SW, tz + 4);
-        if (rc) return rc;
+        if ((rc = make_tensor_map_2d(&e->map_curr[i], e->wave(i), e->nx, e->nz, e->ldx, AC_SW,
+                                     tz + 4)) ||
+            (rc = make_tensor_map_2d(&e->map_prev[i], e->wave(i), e->nx, e->nz, e->ldx, AC_TX, tz)))
+            return rc;
     }
+    for (int i = 0; i < 2; ++i)
+        if ((rc = make_tensor_map_2d(&e->map_vel[i], e->v2dt2.p + (size_t)i * e->plane, e->nx,
+                                     e->nz, e->ldx, AC_TX, tz)))
+            return rc;
+    e->map_sponge = e->map_vel[0];
+    if (e->use_arr && (rc = make_tensor_map_2d(&e->map_sponge, e->sponge_arr.p, e->nx, e->nz,
+                                               e->ldx, AC_TX, tz)))
+        return rc;
     e->tm_tz = tz;
+    return W2D_OK;
+}
+
+int sponge_mode(const w2d_engine* e)
+{
+    return e->use_arr ? SPONGE_ARRAY : (e->use_lut ? SPONGE_LUT : SPONGE_NONE);
+}
+
+// One fused step launch: curr/prev are wave-plane indices, slot the velocity model.
+int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcStep& s)
+{
+    AcMaps m;
+    m.curr = e->map_curr[curr];
+    m.prev = e->map_prev[prev];
+    m.vel = e->map_vel[slot];
+    m.sponge = e->map_sponge;
+    W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), m, g, s, e->stream));
+    e->last_launches++;
     return W2D_OK;
 }
 
@@ -164,7 +196,6 @@ AcGeom geom(w2d_engine* e)
     g.free_surface = e->fs;
     g.n_sponge = e->n_sponge;
     g.sponge_lut = e->use_lut ? e->sponge_lut.p : nullptr;
-    g.sponge_arr = e->use_arr ? e->sponge_arr.p : nullptr;
     g.rec_ptr = e->rec_ptr.p;
     g.rec_list = e->rec_list.p;
     g.shot = e->shot.p;
@@ -200,11 +231,10 @@ int set_shot(w2d_engine* e, int src_ix, int src_iz, const int* rec_ix, int n_rec
     return W2D_OK;
 }
 
-AcStep base_step(w2d_engine* e, int slot)
+AcStep base_step(w2d_engine* e)
 {
     AcStep s;
     memset(&s, 0, sizeof s);
-    s.v2dt2 = e->v2dt2.p + (size_t)slot * e->plane;
     s.dt2_inj = (float)(e->dt_d * e->dt_d);
     s.err = e->err.p;
     return s;
@@ -237,8 +267,7 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
             W2D_CUDA_TRY(cudaMemcpyAsync(c + 2 * e->plane, next, e->plane * 4,
                                          cudaMemcpyDeviceToDevice, e->stream));
         }
-        AcStep s = base_step(e, slot);
-        s.p_prev = prev;
+        AcStep s = base_step(e);
         s.p_next = next;
         s.dt2_inj = dt2inj_f;
         if (it + 1 < o.nt) s.inj_w = e->cur_w + it + 1;
@@ -247,11 +276,12 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
             if (o.snaps) s.snap_out = o.snaps + (size_t)(it / o.interval - o.slot0) * e->plane;
             if (o.illum) s.illum = e->illum.p;
         }
-        launch_step(e->tile, e->tm[(it + 1) % 3], g, s, e->stream);
-        e->last_launches++;
+        int rc = step(e, (it + 1) % 3, it % 3, slot, g, s);
+        if (rc) return rc;
+        (void)prev;
+        (void)curr;
     }
     (void)dt2inj;
-    W2D_CUDA_TRY(cudaGetLastError());
     return W2D_OK;
 }
 
@@ -275,10 +305,8 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
     const AcGeom g = geom(e);
     for (int it = it_hi; it >= it_lo; --it) {
         const int m = nt - 1 - it;
-        float* prev = e->wave(3 + m % 3);
         float* next = e->wave(3 + (m + 2) % 3);
-        AcStep s = base_step(e, slot);
-        s.p_prev = prev;
+        AcStep s = base_step(e);
         s.p_next = next;
         s.dt2_inj = dt2inj_f;
         if (it >= 1 && n_rec > 0) s.inj_data = e->cur_data + (size_t)(it - 1) * n_rec;
@@ -290,10 +318,9 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
                 s.img_dt = img_dt;
             }
         }
-        launch_step(e->tile, e->tm[3 + (m + 1) % 3], g, s, e->stream);
-        e->last_launches++;
+        int rc = step(e, 3 + (m + 1) % 3, 3 + m % 3, slot, g, s);
+        if (rc) return rc;
     }
-    W2D_CUDA_TRY(cudaGetLastError());
     return W2D_OK;
 }
 

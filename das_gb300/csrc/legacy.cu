@@ -30,7 +30,7 @@ struct LegacyCtx {
     int* rec_ptr = nullptr;
     int rec_cap = 0;
     unsigned* err = nullptr;
-    CUtensorMap tm;
+    AcMaps tm;
     const float* tm_base = nullptr;
     int tm_nx = 0, tm_nz = 0;
 };
@@ -120,7 +120,7 @@ int legacy_acoustic(const float* p_curr, const float* p_prev, float* p_next, con
     float *dc = d, *dprev = d + plane, *dn = d + 2 * plane, *dv = d + 3 * plane,
           *ds = d + 4 * plane, *dvel = d + 5 * plane;
     if (g.tm_base != dc || g.tm_nx != nx || g.tm_nz != nz) {
-        if ((rc = make_tensor_map_2d(&g.tm, dc, nx, nz, ldx, AC_SW, 32 + 4))) return rc;
+        if ((rc = make_ac_maps(&g.tm, dc, dprev, dv, ds, nx, nz, ldx, 32))) return rc;
         g.tm_base = dc;
         g.tm_nx = nx;
         g.tm_nz = nz;
@@ -138,18 +138,17 @@ int legacy_acoustic(const float* p_curr, const float* p_prev, float* p_next, con
     geo.inv_dx2 = 1.0f / (dx * dx);
     geo.inv_dz2 = 1.0f / (dz * dz);
     geo.free_surface = fs ? 1 : 0;
-    geo.sponge_arr = sponge ? ds : nullptr;
     geo.rec_ptr = g.rec_ptr;
     geo.rec_list = g.rec_ptr;
     geo.shot = g.shot;
     AcStep s;
     memset(&s, 0, sizeof s);
-    s.p_prev = dprev;
     s.p_next = dn;
-    s.v2dt2 = dv;
     s.err = g.err;
-    launch_acoustic_step<8, 4>(g.tm, geo, s, g.st);
-    W2D_CUDA_TRY(cudaGetLastError());
+    if (sponge)
+        W2D_CUDA_TRY((launch_acoustic_step<8, 4, SPONGE_ARRAY>(g.tm, geo, s, g.st)));
+    else
+        W2D_CUDA_TRY((launch_acoustic_step<8, 4, SPONGE_NONE>(g.tm, geo, s, g.st)));
     if ((rc = download(p_next, 0, dn, nx, nz, ldx))) return rc;
     unsigned h = 0;
     W2D_CUDA_TRY(cudaMemcpyAsync(&h, g.err, 4, cudaMemcpyDeviceToHost, g.st));

@@ -45,7 +45,32 @@ inline int pitch_for(int nx) { return round_up(nx, 32); }
 // Device error-flag bits (written by kernels, read by the host after a pass).
 enum ErrBits : unsigned {
     ERR_TMA_TIMEOUT = 1u,
+    ERR_DEP_TIMEOUT = 2u,  // a persistent CTA waited too long for a neighbour tile
+    ERR_ABORT = 4u,        // set with any error: persistent CTAs stop taking work
 };
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Order this thread's generic-proxy view of global / shared memory before its
+// subsequent async-proxy (TMA) operations.
+__device__ __forceinline__ void fence_proxy_async_global()
+{
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 // ---- PTX helpers (sm_100+ family; compiled for sm_103a) ---------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p)

@@ -145,6 +145,52 @@ int w2d_device_pci_bus_id(char* buf, int len);
 int w2d_host_alloc(void** out, unsigned long long bytes);
 void w2d_host_free(void* p);
 
+/* ---- Part 3: batched / continuously fed migration (no reference counterpart:
+ * the reference migrates shots one after another, rtm_engine.py:125-143) ----- */
+
+/* One shot's migration job: grid, Cerjan sponge parameters (n_sponge < 0: no
+ * sponge), models (vel_fwd = sediment flood, vel_bwd = rock flood), wavelet (nt),
+ * data (nt, n_rec), receiver columns; host arrays, copied at submission. */
+typedef struct {
+    int nx, nz;
+    float dx, dz;
+    double dt;
+    int free_surface;
+    int n_sponge;
+    float sponge_alpha;
+    int nt, snapshot_interval, n_rec;
+    int src_ix, src_iz, rec_iz;
+    const float* vel_fwd;
+    const float* vel_bwd;
+    const float* wavelet;
+    const float* data;
+    const int* rec_ix;
+} w2d_shot_desc;
+
+typedef struct w2d_batch w2d_batch;
+
+/* arena_bytes: device memory for admitted shots (0 = 80 % of free memory). */
+int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_shots);
+void w2d_batch_destroy(w2d_batch* b);
+/* Tile shape of the persistent kernel, phase steps per launch, launches per graph. */
+int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_per_launch,
+                         int launches_per_graph);
+/* Device bytes one shot needs (upper bound) and the largest free arena block. */
+unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d);
+unsigned long long w2d_batch_free_bytes(w2d_batch* b);
+/* Admit a shot; W2D_ENOMEM when it does not fit now (retry after a fetch). */
+int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out);
+/* Replay the captured time loop once over all active shots. */
+int w2d_batch_step(w2d_batch* b, int* n_finished);
+/* 1 finished, 0 running, -1 unused slot. */
+int w2d_batch_is_finished(w2d_batch* b, int slot);
+/* Copy a finished shot's image and illumination (nz, nx) out and free its memory. */
+int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out);
+int w2d_batch_cancel(w2d_batch* b, int slot);
+/* Active shots, device ms / counted point-updates / launches of the last step call. */
+int w2d_batch_stats(w2d_batch* b, int* n_active, float* last_ms, double* last_points,
+                    long long* last_launches);
+
 /* Bytes of device memory the engine may use for snapshots/checkpoints (0 = 80 %
  * of free memory at the time of the call). */
 int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes);

@@ -187,7 +187,8 @@ CASES = [
     (70, 300, 20, True, (3, 150), 3, 2, (4, 8)),
     (65, 129, 12, False, (5, 64), 7, 3, (8, 8)),
     (50, 200, 15, True, (2, 1), 2, 2, (4, 4)),
-    (33, 131, 10, True, (40 - 40 + 2, 130), 2, 4, (16, 4)),
+    (33, 131, 10, True, (2, 130), 2, 4, (8, 8)),
+    (300, 700, 40, True, (2, 350), 2, 2, (8, 4)),
 ]
 
 
