@@ -65,6 +65,10 @@ _SIGS = {
     "w2d_device_pci_bus_id": (c_int, [ctypes.c_char_p, c_int]),
     "w2d_host_alloc": (c_int, [ctypes.POINTER(c_void_p), c_ull]),
     "w2d_host_free": (None, [c_void_p]),
+    "w2d_fwi_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
+                                c_int, c_void_p]),
+    "w2d_fwi_gradient": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "w2d_engine_synchronize": (c_int, [c_void_p]),
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),

@@ -1,0 +1,155 @@
+// adjoint_kernels.cuh -- discrete adjoint of the fused acoustic step, for the
+// velocity gradient of a least-squares misfit (RTM as the adjoint).
+//
+// Forward step (interior cells i, acoustic_kernels.cuh):
+//     P[n+1]_i = s_i * (2 P[n]_i - P[n-1]_i + c_i (L P[n])_i),   c = v^2 dt^2,
+// rows 0 and 1 with a free surface: P[n+1][0,:] = 0, P[n+1][1,x] = -P[n+1][2,x];
+// traces d[n] = P[n+1] at the receivers (before the next injection).
+//
+// With residual traces r[n] (dJ/dd[n]) the adjoint of P[n] is
+//     Lam[n] = S^T r[n-1] + 2 a[n+1] + L^T(c a[n+1]) - a[n+2],
+// where a[n] = s * mu[n] on interior cells (zero elsewhere) and mu[n] is Lam[n]
+// restricted to the interior with the free-surface fold mu[2,x] = Lam[2,x] -
+// Lam[1,x].  L is the same symmetric 4th-order stencil, so L^T(c a) is the
+// stencil applied to the product c*a (zero outside the interior).  The gradient
+// with respect to c accumulates in the same pass:
+//     dJ/dc_i = sum_n a[n+1]_i (L P[n])_i.
+// Sources and receivers must sit on written cells (interior, or rows 0/1 with
+// the free surface) so that the reference's never-written cells stay zero and
+// the step is linear in the wavefields.
+#pragma once
+
+#include "acoustic_kernels.cuh"
+
+namespace w2d {
+
+struct AdjStep {
+    float* a_out;            // a[n]
+    float* grad;             // += a[n+1] * (L P[n]) on interior cells, or null
+    const float* resid_row;  // r[n-1] (n_rec), or null
+    unsigned* err;
+};
+
+struct AdjMaps {
+    CUtensorMap a1;   // a[n+1], halo box
+    CUtensorMap c;    // v^2 dt^2, halo box
+    CUtensorMap pf;   // forward field P[n], halo box
+    CUtensorMap a2;   // a[n+2], plain box
+};
+
+template <int WARPS, int RPW>
+struct AdjTile {
+    static constexpr int TZ = WARPS * RPW;
+    static constexpr int H_FLOATS = (TZ + 4) * AC_SW;
+    static constexpr int P_FLOATS = TZ * AC_TX;
+    static constexpr int FLOATS = 3 * H_FLOATS + P_FLOATS;
+    static constexpr unsigned TX_BYTES = FLOATS * 4u;
+    static constexpr size_t SMEM_BYTES = FLOATS * 4u + 128;
+};
+
+// Laplacian (x part * inv_dx2 + z part * inv_dz2) of a halo tile at shared-memory
+// row `srow`, column `scol`.
+__device__ __forceinline__ float adj_lap(const float* t, int srow, int scol, float inv_dx2,
+                                         float inv_dz2)
+{
+    const float* p = t + srow * AC_SW + scol;
+    const float lx = lap5(p[-2], p[-1], p[0], p[1], p[2]);
+    const float lz = lap5(p[-2 * AC_SW], p[-AC_SW], p[0], p[AC_SW], p[2 * AC_SW]);
+    return lx * inv_dx2 + lz * inv_dz2;
+}
+
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32)
+    acoustic_adjoint_kernel(const __grid_constant__ AdjMaps maps, const AcGeom g, const AdjStep s)
+{
+    static_assert(RPW >= 3, "free-surface rows 0..2 must belong to one warp");
+    using T = AdjTile<WARPS, RPW>;
+    extern __shared__ __align__(128) float smem[];
+    float* ta1 = smem;
+    float* tb = smem + T::H_FLOATS;  // c, then c * a[n+1]
+    float* tp = smem + 2 * T::H_FLOATS;
+    float* ta2 = smem + 3 * T::H_FLOATS;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
+    const int x0 = blockIdx.x * AC_TX;
+    const int z0 = blockIdx.y * T::TZ;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(bar, T::TX_BYTES);
+        tma_load_2d(ta1, &maps.a1, x0 - AC_HX, z0 - 2, bar);
+        tma_load_2d(tb, &maps.c, x0 - AC_HX, z0 - 2, bar);
+        tma_load_2d(tp, &maps.pf, x0 - AC_HX, z0 - 2, bar);
+        tma_load_2d(ta2, &maps.a2, x0, z0, bar);
+    }
+    __syncthreads();
+    if (!mbar_wait_bounded(bar, 0)) {
+        if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    for (int i = threadIdx.x; i < T::H_FLOATS; i += blockDim.x) tb[i] = tb[i] * ta1[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nx = g.nx, nz = g.nz, ldx = g.ldx;
+    const int ixb = x0 + 4 * lane;
+    const int zr0 = z0 + warp * RPW;
+    const int rec_iz = g.shot[2];
+    float lam_row1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int iz = zr0 + r;
+        if (iz >= nz) break;
+        const int srow = warp * RPW + r + 2;
+        const bool row_interior = iz >= 2 && iz < nz - 2;
+        const bool need_row = row_interior || (g.free_surface && iz == 1);
+        if (!need_row) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int ix = ixb + j;
+            if (ix >= nx) continue;
+            const int scol = AC_HX + 4 * lane + j;
+            const float a1 = ta1[srow * AC_SW + scol];
+            const float a2 = ta2[(srow - 2) * AC_TX + 4 * lane + j];
+            float lam = 2.0f * a1 + adj_lap(tb, srow, scol, g.inv_dx2, g.inv_dz2) - a2;
+            if (s.resid_row && iz == rec_iz) {
+                const int k0 = __ldg(g.rec_ptr + ix), k1 = __ldg(g.rec_ptr + ix + 1);
+                for (int k = k0; k < k1; ++k) lam += __ldg(s.resid_row + __ldg(g.rec_list + k));
+            }
+            const bool interior = row_interior && ix >= 2 && ix < nx - 2;
+            if (!interior) {
+                if (iz == 1) lam_row1[j] = lam;  // free-surface row feeds the fold of row 2
+                continue;
+            }
+            if (g.free_surface && iz == 2) lam -= lam_row1[j];
+            float sp = 1.0f;
+            if (g.sponge_lut) {
+                const int d = sponge_dist(ix, iz, nx, nz, g.n_sponge, g.free_surface);
+                if (d > 0) sp = __ldg(g.sponge_lut + d);
+            }
+            const size_t off = (size_t)iz * ldx + ix;
+            s.a_out[off] = sp * lam;
+            if (s.grad)
+                s.grad[off] += a1 * adj_lap(tp, srow, scol, g.inv_dx2, g.inv_dz2);
+        }
+    }
+}
+
+template <int WARPS, int RPW>
+inline cudaError_t launch_adjoint_step(const AdjMaps& m, const AcGeom& g, const AdjStep& s,
+                                       cudaStream_t st)
+{
+    using T = AdjTile<WARPS, RPW>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(acoustic_adjoint_kernel<WARPS, RPW>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)T::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
+    acoustic_adjoint_kernel<WARPS, RPW><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
+    return cudaGetLastError();
+}
+
+}  // namespace w2d

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "acoustic_kernels.cuh"
+#include "adjoint_kernels.cuh"
 #include "small_kernels.cuh"
 #include "w2d_common.cuh"
 #include "wave2d_cuda.h"
@@ -90,7 +91,7 @@ struct w2d_engine {
     size_t plane = 0;  // floats per pitched field
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    TileShape tile{8, 4};
+    TileShape tile{4, 4};
 
     int n_sponge = 0;
     DevBuf<float> sponge_lut, sponge_arr;
@@ -124,6 +125,8 @@ struct w2d_engine {
     int last_storage = 0;
     long long last_launches = 0, last_recompute = 0;
     float last_ms = 0.f;
+
+    struct w2d_fwi_state* fwi = nullptr;  // differentiable-path state (checkpoints, gradient)
 
     float* wave(int i) { return waves.p + (size_t)i * plane; }
 };
@@ -498,7 +501,7 @@ int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
 {
     W2D_CHECK_ARG(e, "engine is NULL");
     if (warps == 0 && rows_per_warp == 0) {
-        warps = 8;
+        warps = 4;
         rows_per_warp = 4;
     }
     W2D_CHECK_ARG(tile_supported(warps, rows_per_warp), "unsupported tile shape");
@@ -902,6 +905,181 @@ int w2d_engine_last_stats(w2d_engine* e, int* storage_used, long long* step_laun
     if (step_launches) *step_launches = e->last_launches;
     if (recomputed_steps) *recomputed_steps = e->last_recompute;
     if (device_ms) *device_ms = e->last_ms;
+    return W2D_OK;
+}
+
+}  // extern "C"
+
+// ---- differentiable forward modelling and its adjoint (velocity gradient) -----
+
+namespace {
+
+// contiguous (nz, nx) velocity on the device -> pitched vel and vel^2 dt^2
+__global__ void fwi_model_kernel(float* v2dt2, float* vel_p, const float* vel, int nx, int nz,
+                                 int ldx, float dt2)
+{
+    const size_t n = (size_t)ldx * nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / ldx), ix = (int)(i % ldx);
+        const float v = ix < nx ? vel[(size_t)iz * nx + ix] : 0.0f;
+        vel_p[i] = v;
+        v2dt2[i] = fmul(fmul(v, v), dt2);
+    }
+}
+
+// dJ/dv = dJ/dc * 2 v dt^2, pitched -> contiguous
+__global__ void fwi_chain_kernel(float* grad_v, const float* grad_c, const float* vel_p, int nx,
+                                 int nz, int ldx, float dt2)
+{
+    const size_t n = (size_t)nx * nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / nx), ix = (int)(i % nx);
+        const size_t o = (size_t)iz * ldx + ix;
+        grad_v[i] = grad_c[o] * 2.0f * vel_p[o] * dt2;
+    }
+}
+
+bool written_cell(const w2d_engine* e, int iz, int ix)
+{
+    const bool interior = iz >= 2 && iz < e->nz - 2 && ix >= 2 && ix < e->nx - 2;
+    return interior || (e->fs && iz >= 0 && iz < 2 && ix >= 0 && ix < e->nx);
+}
+
+}  // namespace
+
+struct w2d_fwi_state {
+    int nt = 0, n_rec = 0, seg = 0, n_seg = 0;
+    DevBuf<float> vel_p, grad_c, zero, segbuf;
+    std::vector<CUtensorMap> seg_maps;
+    CUtensorMap map_c_halo, map_zero;
+};
+
+extern "C" {
+
+int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, int nt, int src_ix,
+                    int src_iz, const int* rec_ix, int n_rec, int rec_iz, float* traces_dev)
+{
+    int rc;
+    if ((rc = common_checks(e, nt, 1))) return rc;
+    W2D_CHECK_ARG(vel_dev && wavelet && traces_dev, "NULL argument");
+    W2D_CHECK_ARG(n_rec > 0 && rec_ix, "receivers required");
+    W2D_CHECK_ARG(e->tile.rpw == 4 && (e->tile.warps == 4 || e->tile.warps == 8),
+                  "the adjoint path runs with 4x4 or 8x4 tiles");
+    W2D_CHECK_ARG(src_ix >= 0 && src_ix < e->nx && src_iz >= 0 && src_iz < e->nz &&
+                      written_cell(e, src_iz, src_ix),
+                  "the source must sit on a written cell (interior or free-surface rows)");
+    for (int r = 0; r < n_rec; ++r)
+        W2D_CHECK_ARG(rec_ix[r] >= 0 && rec_ix[r] < e->nx && written_cell(e, rec_iz, rec_ix[r]),
+                      "receivers must sit on written cells (interior or free-surface rows)");
+    if (!e->fwi) e->fwi = new w2d_fwi_state();
+    w2d_fwi_state* f = e->fwi;
+    if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
+    f->nt = nt;
+    f->n_rec = n_rec;
+    f->seg = std::max(1, (int)std::sqrt(3.0 * nt));
+    f->n_seg = (nt + f->seg - 1) / f->seg;
+    if ((rc = f->vel_p.ensure(e->plane)) || (rc = f->grad_c.ensure(e->plane)) ||
+        (rc = f->zero.ensure(e->plane)) || (rc = f->segbuf.ensure((size_t)f->seg * e->plane)) ||
+        (rc = e->ckpt.ensure((size_t)f->n_seg * 3 * e->plane)) || (rc = e->wavelet.ensure(nt)) ||
+        (rc = e->rec_out.ensure((size_t)nt * n_rec)) || (rc = e->data.ensure((size_t)nt * n_rec)))
+        return rc;
+    W2D_CUDA_TRY(cudaMemsetAsync(f->zero.p, 0, e->plane * 4, e->stream));
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet.p, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice,
+                                 e->stream));
+    fwi_model_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->v2dt2.p, f->vel_p.p, vel_dev,
+                                                               e->nx, e->nz, e->ldx, e->dt2);
+    W2D_CUDA_TRY(cudaGetLastError());
+    e->vel_set[0] = true;
+    e->cur_w = e->wavelet.p;
+    e->last_launches = 0;
+    e->last_recompute = 0;
+    const float dt2inj = (float)(e->dt_d * e->dt_d);
+    if ((rc = forward_begin(e, dt2inj))) return rc;
+    FwdOpts o;
+    o.nt = nt;
+    o.n_rec = n_rec;
+    o.rec_out = e->rec_out.p;
+    o.ckpt = e->ckpt.p;
+    o.ckpt_every = f->seg;
+    if ((rc = run_forward_steps(e, 0, o, 0, nt, 0.0, dt2inj))) return rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(traces_dev, e->rec_out.p, (size_t)nt * n_rec * 4,
+                                 cudaMemcpyDeviceToDevice, e->stream));
+    return check_err(e);
+}
+
+int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
+{
+    W2D_CHECK_ARG(e && e->fwi && e->fwi->nt > 0, "call w2d_fwi_forward first");
+    W2D_CHECK_ARG(resid_dev && grad_dev, "NULL argument");
+    w2d_fwi_state* f = e->fwi;
+    const int nt = f->nt, n_rec = f->n_rec, seg = f->seg;
+    const size_t plane_b = e->plane * 4;
+    int rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, resid_dev, (size_t)nt * n_rec * 4,
+                                 cudaMemcpyDeviceToDevice, e->stream));
+    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * plane_b, e->stream));
+    W2D_CUDA_TRY(cudaMemsetAsync(f->grad_c.p, 0, plane_b, e->stream));
+    const int hz = e->tile.tz() + 4;
+    if ((rc = make_tensor_map_2d(&f->map_c_halo, e->v2dt2.p, e->nx, e->nz, e->ldx, AC_SW, hz)) ||
+        (rc = make_tensor_map_2d(&f->map_zero, f->zero.p, e->nx, e->nz, e->ldx, AC_SW, hz)))
+        return rc;
+    f->seg_maps.resize(seg);
+    for (int k = 0; k < seg; ++k)
+        if ((rc = make_tensor_map_2d(&f->seg_maps[k], f->segbuf.p + (size_t)k * e->plane, e->nx,
+                                     e->nz, e->ldx, AC_SW, hz)))
+            return rc;
+    const AcGeom g = geom(e);
+    auto adj = [&](int n, const CUtensorMap& pf) -> int {
+        AdjMaps m;
+        m.a1 = e->map_curr[3 + (n + 1) % 3];
+        m.a2 = e->map_prev[3 + (n + 2) % 3];
+        m.c = f->map_c_halo;
+        m.pf = pf;
+        AdjStep s;
+        s.a_out = e->wave(3 + n % 3);
+        s.grad = f->grad_c.p;
+        s.resid_row = n >= 1 ? e->data.p + (size_t)(n - 1) * n_rec : nullptr;
+        s.err = e->err.p;
+        cudaError_t ce = e->tile.warps == 4 ? launch_adjoint_step<4, 4>(m, g, s, e->stream)
+                                            : launch_adjoint_step<8, 4>(m, g, s, e->stream);
+        W2D_CUDA_TRY(ce);
+        e->last_launches++;
+        return W2D_OK;
+    };
+    e->last_launches = 0;
+    e->last_recompute = 0;
+    if ((rc = adj(nt, f->map_zero))) return rc;
+    const float dt2inj = (float)(e->dt_d * e->dt_d);
+    for (int sgi = f->n_seg - 1; sgi >= 0; --sgi) {
+        const int a = sgi * seg, b = std::min(nt, a + seg);
+        const float* c = e->ckpt.p + (size_t)sgi * 3 * e->plane;
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave(a % 3), c, plane_b, cudaMemcpyDeviceToDevice, e->stream));
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 1) % 3), c + e->plane, plane_b,
+                                     cudaMemcpyDeviceToDevice, e->stream));
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 2) % 3), c + 2 * e->plane, plane_b,
+                                     cudaMemcpyDeviceToDevice, e->stream));
+        FwdOpts r;
+        r.nt = nt;
+        r.interval = 1;
+        r.snaps = f->segbuf.p;
+        r.slot0 = a;
+        if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
+        e->last_recompute += b - a;
+        for (int n = b - 1; n >= a; --n)
+            if ((rc = adj(n, f->seg_maps[n - a]))) return rc;
+    }
+    fwi_chain_kernel<<<grid_for((size_t)e->nx * e->nz), 256, 0, e->stream>>>(
+        grad_dev, f->grad_c.p, f->vel_p.p, e->nx, e->nz, e->ldx, e->dt2);
+    W2D_CUDA_TRY(cudaGetLastError());
+    return check_err(e);
+}
+
+int w2d_engine_synchronize(w2d_engine* e)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
     return W2D_OK;
 }
 

@@ -145,6 +145,20 @@ int w2d_device_pci_bus_id(char* buf, int len);
 int w2d_host_alloc(void** out, unsigned long long bytes);
 void w2d_host_free(void* p);
 
+/* ---- Differentiable modelling (no reference counterpart: RTM as the adjoint) ----
+ * Forward modelling in velocity vel_dev (DEVICE, contiguous nz x nx float32),
+ * traces written to traces_dev (DEVICE, nt x n_rec), checkpoints of the forward
+ * state kept in the engine.  Source and receivers must sit on written cells
+ * (interior, or rows 0/1 with the free surface). */
+int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, int nt, int src_ix,
+                    int src_iz, const int* rec_ix, int n_rec, int rec_iz, float* traces_dev);
+/* Gradient of sum(resid * traces) with respect to the velocity of the last
+ * w2d_fwi_forward on this engine: resid_dev (DEVICE, nt x n_rec), grad_dev
+ * (DEVICE, nz x nx, overwritten).  Hand-written adjoint kernel; the forward
+ * wavefield is recomputed segment by segment from the checkpoints. */
+int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev);
+int w2d_engine_synchronize(w2d_engine* e);
+
 /* ---- Part 3: batched / continuously fed migration (no reference counterpart:
  * the reference migrates shots one after another, rtm_engine.py:125-143) ----- */
 
