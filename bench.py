@@ -339,7 +339,7 @@ def run_ours(args, dist):
                "config": {"workload": sv.name, "nz": sv.nz, "nx": sv.nx, "nt": sv.nt,
                           "dx": sv.dx, "dt": sv.dt, "receivers": int(len(sv.rec_ix)),
                           "shots_per_step": 1, "snapshot_interval": interval,
-                          "storage": used, "tile": list(solver.tile or (8, 4)),
+                          "storage": used, "tile": list(solver.tile or (4, 4)),
                           "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
                "shots_per_s": K * dist.world / dev_s,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -80,4 +80,4 @@ def test_gradient_relates_to_rtm_image():
     m = (slice(8, 40), slice(12, 88))
     c = np.corrcoef(g[m].ravel(), img[m].ravel())[0, 1]
     print(f"correlation(gradient, RTM image of the residual) = {c:.3f}")
-    assert abs(c) > 0.3
+    assert c < -0.6  # d2/dt2 ~ -omega^2: anti-correlated with the zero-lag image
