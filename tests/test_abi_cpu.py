@@ -9,17 +9,25 @@ import pytest
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    with open(os.path.join(REPO, "include", "wave2d_cuda.h")) as f:
+def header_functions(name="wave2d_cuda.h"):
+    with open(os.path.join(REPO, "include", name)) as f:
         text = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
     return sorted(set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\(", text)) - {"if", "sizeof"})
+
+
+def all_header_functions():
+    import glob
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        names.update(header_functions(os.path.basename(h)))
+    return sorted(names)
 
 
 def test_library_builds_and_exports_header_symbols():
     from das_gb300 import build
     path = build.build()
     lib = ctypes.CDLL(path)  # loading needs no GPU
-    names = header_functions()
+    names = all_header_functions()
     assert "acoustic_2d_step" in names and "w2d_migrate_shot" in names
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
