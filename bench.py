@@ -381,7 +381,11 @@ def run_batched(args, dist):
     from das_gb300.wave_solver import WaveSolver2D
     jobs = _batched_jobs(args.batch_shots, seed=0, nt_scale=args.batch_nt_scale)
     pts = sum(j.counted_points for j in jobs)
-    tile = tuple(int(t) for t in (args.tile or "8,4").split(","))
+    tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
+    tune_table = None
+    if args.autotune:
+        from das_gb300.autotune import tune_batch
+        (tile, args.spl, args.lpg), tune_table = tune_batch(jobs, use_cache=False)
     eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=len(jobs), tile=tile,
                       steps_per_launch=args.spl, launches_per_graph=args.lpg)
     eng.run(jobs[: min(4, len(jobs))])  # warm-up: graph capture, first-touch of the arena
@@ -413,7 +417,8 @@ def run_batched(args, dist):
            "wall_s": wall, "max_active_shots": st["max_active"],
            "plain_loop": {"shots": k, "shots_per_s": k / plain_s,
                           "gpts_per_s": plain_pts / plain_s / 1e9},
-           "speedup_vs_plain_loop_gpts": (pts / wall) / (plain_pts / plain_s)}
+           "speedup_vs_plain_loop_gpts": (pts / wall) / (plain_pts / plain_s),
+           "autotune": tune_table}
     print(json.dumps(out), flush=True)
 
 
@@ -427,6 +432,7 @@ def main():
     ap.add_argument("--arena-gb", type=float, default=200.0)
     ap.add_argument("--spl", type=int, default=16)
     ap.add_argument("--lpg", type=int, default=16)
+    ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

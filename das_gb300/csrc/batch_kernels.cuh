@@ -74,8 +74,10 @@ __device__ __forceinline__ bool wait_counter(const unsigned* p, unsigned target,
     return false;
 }
 
+// Registers capped so that four 256-thread (or eight 128-thread) CTAs fit per SM.
 template <int WARPS, int RPW>
-__global__ void __launch_bounds__(WARPS * 32) acoustic_batch_kernel(const BatchArgs a)
+__global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1)
+    acoustic_batch_kernel(const BatchArgs a)
 {
     using T = AcTile<WARPS, RPW, SPONGE_LUT>;
     extern __shared__ __align__(128) float smem[];
@@ -83,24 +85,26 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_kernel(const BatchA
     __shared__ int s_item;
     __shared__ int s_ok;
     const int tid = threadIdx.x;
+    const int n_act = *a.n_active;
+    if (n_act <= 0) return;
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
+        s_item = (int)atomicAdd(a.head, 1u);
     }
-    __syncthreads();
-    const int n_act = *a.n_active;
-    if (n_act <= 0) return;
     const int T_all = a.tile_prefix[n_act];
     const long long total = (long long)a.S * T_all;
     unsigned phase = 0;
+    // The next queue index is taken while the current item is processed, which
+    // hides the atomic's round trip.  Items are still processed in increasing
+    // order per CTA, so every awaited item is held by a CTA that reaches it.
+    int next = 0;
     for (;;) {
-        if (tid == 0) {
-            s_item = (int)atomicAdd(a.head, 1u);
-            s_ok = (*reinterpret_cast<volatile unsigned*>(a.err) & ERR_ABORT) ? 0 : 1;
-        }
+        if (tid == 0) s_ok = (*reinterpret_cast<volatile unsigned*>(a.err) & ERR_ABORT) ? 0 : 1;
         __syncthreads();
         const long long item = s_item;
         if (item >= total || !s_ok) break;
+        if (tid == 0) next = (int)atomicAdd(a.head, 1u);
         const int j = (int)(item / T_all);
         const int r = (int)(item - (long long)j * T_all);
         int lo = 0, hi = n_act - 1;
@@ -114,6 +118,7 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_kernel(const BatchA
         const int k = sh->k0 + j;
         if (k >= sh->k_end) {
             __syncthreads();
+            if (tid == 0) s_item = next;
             continue;
         }
         const int tiles_x = sh->tiles_x, tiles_z = sh->tiles_z;
@@ -184,6 +189,7 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_kernel(const BatchA
         if (tid == 0) {
             __threadfence();
             st_release_u32(sh->done + t, (unsigned)(k + 1));
+            s_item = next;
         }
     }
 }

@@ -1,0 +1,153 @@
+"""RTM serving: continuous batching of migration jobs on one GB300.
+
+A job is a list of shots (each a ``ShotJob``: grid, models, wavelet, data,
+receivers) that arrives at some time.  The server keeps every admitted shot's
+wavefields, snapshot store and inputs resident in the batched engine's device
+arena; shots are admitted in arrival order whenever the arena (the HBM budget)
+and a slot have room, so requests that arrive while others are running join
+them on the device between two replays of the captured time loop; finished
+shots leave at once, freeing memory for the next ones.  A job completes when its
+last shot does; its latency is completion time minus arrival time.
+
+Each shot's image and illumination are bit-identical to migrating it alone: the
+persistent kernel applies the same fused step to each tile whatever else is in
+the batch.  Elastic jobs go to ``elastic_executor`` (a callable taking a job
+and returning its per-shot results) between replays when one is given.
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional, Sequence
+
+import numpy as np
+
+from .batch import BatchEngine, ShotJob
+
+
+@dataclass
+class RTMRequest:
+    job_id: int
+    shots: List[ShotJob]
+    arrival: float          # seconds from the start of the trace
+    kind: str = "acoustic"  # "acoustic" or "elastic"
+
+
+@dataclass
+class RTMResponse:
+    job_id: int
+    kind: str
+    arrival: float
+    finished: float
+    results: List[tuple] = field(default_factory=list)
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def percentile(xs: Sequence[float], q: float) -> float:
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else float("nan")
+
+
+class RTMServer:
+    def __init__(self, engine: BatchEngine, elastic_executor: Optional[Callable] = None):
+        self.engine = engine
+        self.elastic_executor = elastic_executor
+
+    def serve(self, trace: Sequence[RTMRequest], realtime: bool = True):
+        """Run a trace of requests to completion; returns (responses, statistics).
+
+        realtime: arrivals follow the wall clock (requests arriving while the GPU
+        works wait in the queue).  Otherwise the clock is the device time of the
+        replays, which makes a run independent of host speed (used by tests).
+        """
+        trace = sorted(trace, key=lambda r: r.arrival)
+        eng = self.engine
+        t_start = time.perf_counter()
+        dev_clock = 0.0
+
+        def now():
+            return time.perf_counter() - t_start if realtime else dev_clock
+
+        queue = collections.deque()  # (request, shot index)
+        running: Dict[int, tuple] = {}
+        responses: Dict[int, RTMResponse] = {}
+        remaining: Dict[int, int] = {}
+        i = 0
+        pts = 0.0
+        busy_ms = 0.0
+        max_active = 0
+        n_shots = 0
+        while i < len(trace) or queue or running:
+            t = now()
+            while i < len(trace) and trace[i].arrival <= t:
+                req = trace[i]
+                responses[req.job_id] = RTMResponse(req.job_id, req.kind, req.arrival, float("nan"),
+                                                    [None] * len(req.shots))
+                remaining[req.job_id] = len(req.shots)
+                if req.kind == "elastic" and self.elastic_executor is not None:
+                    res = self.elastic_executor(req)
+                    responses[req.job_id].results = list(res)
+                    remaining[req.job_id] = 0
+                    responses[req.job_id].finished = now()
+                else:
+                    for k in range(len(req.shots)):
+                        queue.append((req, k))
+                i += 1
+            while queue:  # admission in arrival order, by memory and slots
+                req, k = queue[0]
+                slot = eng.submit(req.shots[k])
+                if slot is None:
+                    break
+                queue.popleft()
+                running[slot] = (req, k)
+            if not running:
+                if queue:
+                    raise MemoryError(f"job {queue[0][0].job_id}: a shot does not fit the arena")
+                if i < len(trace):
+                    if realtime:
+                        time.sleep(max(0.0, trace[i].arrival - now()))
+                    else:
+                        dev_clock = max(dev_clock, trace[i].arrival)
+                continue
+            max_active = max(max_active, len(running))
+            eng.step()
+            busy_ms += eng.last_ms
+            pts += eng.last_points
+            dev_clock += eng.last_ms / 1e3
+            for slot in [s for s in running if eng.finished(s)]:
+                req, k = running.pop(slot)
+                sh = req.shots[k]
+                responses[req.job_id].results[k] = eng.fetch(slot, sh.nz, sh.nx)
+                n_shots += 1
+                remaining[req.job_id] -= 1
+                if remaining[req.job_id] == 0:
+                    responses[req.job_id].finished = now()
+        makespan = now()
+        out = [responses[r.job_id] for r in trace]
+        lat = [r.latency for r in out]
+        span_jobs = trace[-1].arrival - trace[0].arrival if len(trace) > 1 else 0.0
+        stats = {"jobs": len(out), "shots": sum(len(r.shots) for r in trace),
+                 "makespan_s": makespan, "p50_latency_s": percentile(lat, 50),
+                 "p99_latency_s": percentile(lat, 99),
+                 "shots_per_s": sum(len(r.shots) for r in trace) / makespan if makespan else 0.0,
+                 "gpts_per_s": pts / makespan / 1e9 if makespan else 0.0,
+                 "device_busy_frac": busy_ms / 1e3 / makespan if makespan else 0.0,
+                 "offered_jobs_per_s": (len(trace) - 1) / span_jobs if span_jobs > 0 else None,
+                 "max_active_shots": max_active}
+        return out, stats
+
+
+def poisson_trace(n_jobs: int, rate: float, make_job: Callable[[int, np.random.Generator], tuple],
+                  seed: int = 0) -> List[RTMRequest]:
+    """Requests with exponential inter-arrival times; make_job(i, rng) -> (kind, shots)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n_jobs):
+        t += rng.exponential(1.0 / rate)
+        kind, shots = make_job(i, rng)
+        out.append(RTMRequest(i, shots, t, kind))
+    return out
