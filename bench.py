@@ -422,10 +422,102 @@ def run_batched(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
+    """Poisson arrivals at `rate` jobs/s; grid sides log-uniform from 128 x 256 to
+    1024 x 4096 (times side_scale), nt uniform in [1000, 8000] (times nt_scale), 1-32
+    shots per job sharing the job's smoothed faulted model; 80 % acoustic / 20 % elastic."""
+    from das_gb300.batch import ShotJob
+    from das_gb300.serving import poisson_trace
+    from das_gb300.synthetic import _layered_faulted
+    from das_gb300.wave_solver import ricker_wavelet
+    from scipy.ndimage import gaussian_filter
+
+    def make(i, rng):
+        nz = int(np.exp(rng.uniform(np.log(128), np.log(1024))) * side_scale)
+        nx = int(np.exp(rng.uniform(np.log(256), np.log(4096))) * side_scale)
+        nz, nx = max(nz, 48), max(nx, 96)
+        nt = max(64, int(rng.integers(1000, 8001) * nt_scale))
+        kind = "elastic" if rng.uniform() < 0.2 else "acoustic"
+        d = 5.0
+        zmax = (nz - 1) * d
+        faults = [(rng.uniform(0.2, 0.8) * (nx - 1) * d, rng.uniform(45.0, 80.0),
+                   rng.uniform(-0.08, 0.08) * zmax) for _ in range(int(rng.integers(1, 4)))]
+        v = _layered_faulted(nz, nx, d, d, 0.45 * zmax, 0.12 * zmax, 0.0, faults, v1=3000.0)
+        v = gaussian_filter(v, 3.0).astype(np.float32)
+        dt = 5e-4
+        w, _ = ricker_wavelet(float(rng.uniform(3.0, 5.0)), dt, nt * dt)
+        rix = np.arange(nx)
+        data = (rng.standard_normal((nt, nx)) * 1e-8).astype(np.float32)
+        n_sh = int(rng.integers(1, 33))
+        shots = [ShotJob(nx, nz, d, d, dt, v, v, w, data, rix,
+                         int((k + 0.5) * nx / n_sh), 2, 2, 2, 30, 0.0015, True)
+                 for k in range(n_sh)]
+        return kind, shots
+
+    return poisson_trace(n_jobs, rate, make, seed=seed)
+
+
+def run_served(args, dist):
+    """Served workload: continuous batching server vs the plain per-shot loop (FIFO)."""
+    from das_gb300.batch import BatchEngine
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.serving import RTMServer, percentile
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D
+    trace = _served_trace(args.serve_jobs, args.serve_rate, 0, args.serve_side_scale,
+                          args.serve_nt_scale)
+    n_el = sum(r.kind == "elastic" for r in trace)
+    tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
+    eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=4096, tile=tile,
+                      steps_per_launch=args.spl, launches_per_graph=args.lpg)
+    eng.run(trace[0].shots[:1])  # graph capture, first touch
+    out, st = RTMServer(eng).serve(trace, realtime=True)
+    eng.close()
+    # plain per-shot loop over the first jobs of the same trace, arrivals on the wall clock
+    m = min(args.plain_jobs, len(trace))
+    t0 = time.perf_counter()
+    lat, shots_done = [], 0
+    for r in trace[:m]:
+        wait = r.arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        j0 = r.shots[0]
+        s = WaveSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha, True)
+        e = TSWRTMEngine(s, "all")
+        fm = FloodModels(j0.vel_fwd, j0.vel_fwd, j0.vel_bwd, 0, 0)
+        for j in r.shots:
+            e.migrate_shot(fm, j.wavelet, j.source_ix, j.source_iz, j.data, j.receiver_ix, 2, 2)
+            shots_done += 1
+        s.close()
+        lat.append(time.perf_counter() - t0 - r.arrival)
+    plain_span = time.perf_counter() - t0
+    plain = {"jobs": m, "shots": shots_done, "shots_per_s": shots_done / plain_span,
+             "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
+    served_first = [x.latency for x in out[:m]]
+    out_line = {"metric": "served RTM shots/s", "value": st["shots_per_s"], "unit": "shots/s",
+                "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": f"Poisson trace of {len(trace)} jobs at {args.serve_rate} "
+                                       f"jobs/s, sides log-uniform 128x256..1024x4096 x "
+                                       f"{args.serve_side_scale}, nt U[1000,8000] x "
+                                       f"{args.serve_nt_scale}, 1-32 shots/job",
+                           "elastic_jobs_in_trace": n_el, "tile": list(tile),
+                           "steps_per_launch": args.spl, "launches_per_graph": args.lpg},
+                "served": st, "plain_loop": plain,
+                "served_first_jobs": {"p50_latency_s": percentile(served_first, 50),
+                                      "p99_latency_s": percentile(served_first, 99)},
+                "speedup_vs_plain_loop_shots": st["shots_per_s"] / plain["shots_per_s"]}
+    print(json.dumps(out_line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", default="large", choices=["large", "batched"])
+    ap.add_argument("--workload", default="large", choices=["large", "batched", "served"])
+    ap.add_argument("--serve-jobs", type=int, default=40)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-side-scale", type=float, default=1.0)
+    ap.add_argument("--serve-nt-scale", type=float, default=1.0)
+    ap.add_argument("--plain-jobs", type=int, default=8)
     ap.add_argument("--batch-shots", type=int, default=256)
     ap.add_argument("--batch-nt-scale", type=float, default=1.0)
     ap.add_argument("--plain-shots", type=int, default=16)
@@ -461,6 +553,8 @@ def main():
     try:
         if args.workload == "batched":
             run_batched(args, dist)
+        elif args.workload == "served":
+            run_served(args, dist)
         else:
             run_ours(args, dist)
     finally:

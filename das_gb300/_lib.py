@@ -76,6 +76,8 @@ _SIGS = {
     "w2d_batch_free_bytes": (c_ull, [c_void_p]),
     "w2d_batch_submit": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
     "w2d_batch_step": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
+    "w2d_batch_launch": (c_int, [c_void_p]),
+    "w2d_batch_wait": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "w2d_batch_is_finished": (c_int, [c_void_p, c_int]),
     "w2d_batch_fetch": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "w2d_batch_cancel": (c_int, [c_void_p, c_int]),

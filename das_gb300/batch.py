@@ -133,8 +133,17 @@ class BatchEngine:
 
     def step(self) -> int:
         """Replay the captured time loop once; returns how many shots finished."""
+        self.launch()
+        return self.wait()
+
+    def launch(self) -> None:
+        """Start one replay; shots submitted meanwhile upload in parallel and join the next."""
+        _lib.check(self._lib.w2d_batch_launch(self._h))
+
+    def wait(self) -> int:
+        """Finish the replay in flight; returns how many shots finished."""
         n = ctypes.c_int(0)
-        _lib.check(self._lib.w2d_batch_step(self._h, ctypes.byref(n)))
+        _lib.check(self._lib.w2d_batch_wait(self._h, ctypes.byref(n)))
         na, ms, pts, la = ctypes.c_int(), ctypes.c_float(), ctypes.c_double(), ctypes.c_longlong()
         _lib.check(self._lib.w2d_batch_stats(self._h, ctypes.byref(na), ctypes.byref(ms),
                                              ctypes.byref(pts), ctypes.byref(la)))
@@ -160,16 +169,24 @@ class BatchEngine:
         pts = 0.0
         launches = 0
         max_active = 0
-        while pending or running:
+
+        def admit():
             while pending:
                 slot = self.submit(jobs[pending[0]])
                 if slot is None:
                     break
                 running[slot] = pending.pop(0)
+
+        admit()
+        while running or pending:
             if not running:
-                raise MemoryError("a shot does not fit in the arena even when it is empty")
+                admit()
+                if not running:
+                    raise MemoryError("a shot does not fit in the arena even when it is empty")
             max_active = max(max_active, len(running))
-            self.step()
+            self.launch()
+            admit()  # uploads overlap the replay in flight; these shots join the next one
+            self.wait()
             dev_ms += self.last_ms
             pts += self.last_points
             launches += self.last_launches

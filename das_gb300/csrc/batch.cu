@@ -44,7 +44,8 @@ struct HostShot {
 }  // namespace
 
 struct w2d_batch {
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;     // replays of the captured time loop
+    cudaStream_t st_up = nullptr;  // shot admission (uploads, set-up kernels)
     char* arena = nullptr;
     size_t arena_bytes = 0;
     std::map<size_t, size_t> free_blocks;  // offset -> bytes
@@ -64,6 +65,9 @@ struct w2d_batch {
     int grid = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<cudaEvent_t> ready;  // per slot: admission work finished
+    std::vector<int> joining;        // admitted shots that join at the next launch
+    bool in_flight = false;
     float last_ms = 0.f;
     double last_pts = 0;
     long long last_launches = 0;
@@ -211,6 +215,7 @@ int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_sh
         arena_bytes = (unsigned long long)(fr * 0.8);
     }
     if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->st_up, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) {
         set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
@@ -238,6 +243,7 @@ int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_sh
     cudaMemset(b->d_prefix, 0, sizeof(int) * (max_shots + 1));
     b->h_shots.resize(max_shots);
     b->hs.resize(max_shots);
+    b->ready.assign(max_shots, nullptr);
     if (cudaDeviceSynchronize() != cudaSuccess) {
         set_error("batch set-up failed");
         return fail(W2D_ECUDA);
@@ -256,6 +262,10 @@ void w2d_batch_destroy(w2d_batch* b)
         if (p) cudaFree(p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    if (b->st_up) cudaStreamSynchronize(b->st_up);
+    for (cudaEvent_t ev : b->ready)
+        if (ev) cudaEventDestroy(ev);
+    if (b->st_up) cudaStreamDestroy(b->st_up);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
 }
@@ -361,7 +371,7 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     int* rptr = reinterpret_cast<int*>(base + o_ptr);
     int* rlist = reinterpret_cast<int*>(base + o_list);
     unsigned* done = reinterpret_cast<unsigned*>(base + o_done);
-    cudaStream_t st = b->st;
+    cudaStream_t st = b->st_up;
     const float dtf = (float)d->dt;
     const float dt2 = dtf * dtf;
     int rc = W2D_OK;
@@ -450,7 +460,13 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     if (n_rec > 0)
         inject_kernel<<<(nx + 255) / 256, 256, 0, st>>>(h.wave[4], h.g, nullptr,
                                                         ddev + (size_t)(nt - 1) * n_rec, h.dt2_inj);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+    if (!b->ready[slot] && cudaEventCreateWithFlags(&b->ready[slot], cudaEventDisableTiming)) {
+        set_error("event creation failed");
+        return undo(W2D_ECUDA);
+    }
+    // the admission work runs on its own stream, overlapping a replay in flight;
+    // the next launch waits for this event before the shot joins
+    if (cudaGetLastError() != cudaSuccess || cudaEventRecord(b->ready[slot], st) != cudaSuccess) {
         set_error("shot admission failed on the device");
         return undo(W2D_ECUDA);
     }
@@ -468,19 +484,24 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     hsh.image = img;
     hsh.illum = ill;
     hsh.counted_pts = 2.0 * nx * nz * nt;
-    b->active.push_back(slot);
-    b->active_dirty = true;
+    b->joining.push_back(slot);
     *slot_out = slot;
     return W2D_OK;
 }
 
-int w2d_batch_step(w2d_batch* b, int* n_finished)
+int w2d_batch_launch(w2d_batch* b)
 {
     W2D_CHECK_ARG(b, "batch is NULL");
-    if (n_finished) *n_finished = 0;
+    W2D_CHECK_ARG(!b->in_flight, "a replay is already in flight");
     b->last_ms = 0.f;
     b->last_pts = 0;
     b->last_launches = 0;
+    for (int s : b->joining) {
+        W2D_CUDA_TRY(cudaStreamWaitEvent(b->st, b->ready[s], 0));
+        b->active.push_back(s);
+        b->active_dirty = true;
+    }
+    b->joining.clear();
     if (b->active.empty()) return W2D_OK;
     int rc;
     if (b->active_dirty) {
@@ -488,18 +509,28 @@ int w2d_batch_step(w2d_batch* b, int* n_finished)
         for (size_t i = 0; i < b->active.size(); ++i)
             prefix[i + 1] = prefix[i] + b->h_shots[b->active[i]].ntiles;
         const int n = (int)b->active.size();
+        // pageable sources: the copies are staged before these calls return
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_active, b->active.data(), n * 4, cudaMemcpyHostToDevice,
                                      b->st));
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_prefix, prefix.data(), (n + 1) * 4,
                                      cudaMemcpyHostToDevice, b->st));
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_nact, &n, 4, cudaMemcpyHostToDevice, b->st));
-        W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
         b->active_dirty = false;
     }
     if (!b->gexec && (rc = build_graph(b))) return rc;
     W2D_CUDA_TRY(cudaEventRecord(b->e0, b->st));
     W2D_CUDA_TRY(cudaGraphLaunch(b->gexec, b->st));
     W2D_CUDA_TRY(cudaEventRecord(b->e1, b->st));
+    b->in_flight = true;
+    return W2D_OK;
+}
+
+int w2d_batch_wait(w2d_batch* b, int* n_finished)
+{
+    W2D_CHECK_ARG(b, "batch is NULL");
+    if (n_finished) *n_finished = 0;
+    if (!b->in_flight) return W2D_OK;
+    b->in_flight = false;
     unsigned herr = 0;
     W2D_CUDA_TRY(cudaMemcpyAsync(&herr, b->d_err, 4, cudaMemcpyDeviceToHost, b->st));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
@@ -539,6 +570,13 @@ int w2d_batch_step(w2d_batch* b, int* n_finished)
     return W2D_OK;
 }
 
+int w2d_batch_step(w2d_batch* b, int* n_finished)
+{
+    int rc;
+    if ((rc = w2d_batch_launch(b))) return rc;
+    return w2d_batch_wait(b, n_finished);
+}
+
 int w2d_batch_is_finished(w2d_batch* b, int slot)
 {
     if (!b || slot < 0 || slot >= b->max_shots || !b->hs[slot].used) return -1;
@@ -566,11 +604,15 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
 int w2d_batch_cancel(w2d_batch* b, int slot)
 {
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
+    W2D_CHECK_ARG(!b->in_flight, "cancel between replays only");
     auto it = std::find(b->active.begin(), b->active.end(), slot);
     if (it != b->active.end()) {
         b->active.erase(it);
         b->active_dirty = true;
     }
+    auto jt = std::find(b->joining.begin(), b->joining.end(), slot);
+    if (jt != b->joining.end()) b->joining.erase(jt);
+    W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
     arena_free(b, b->hs[slot].off, b->hs[slot].bytes);
     b->hs[slot] = HostShot();

@@ -80,7 +80,8 @@ class RTMServer:
         busy_ms = 0.0
         max_active = 0
         n_shots = 0
-        while i < len(trace) or queue or running:
+        def intake():
+            nonlocal i
             t = now()
             while i < len(trace) and trace[i].arrival <= t:
                 req = trace[i]
@@ -96,13 +97,19 @@ class RTMServer:
                     for k in range(len(req.shots)):
                         queue.append((req, k))
                 i += 1
-            while queue:  # admission in arrival order, by memory and slots
+
+        def admit():  # arrival order, by memory and slots
+            while queue:
                 req, k = queue[0]
                 slot = eng.submit(req.shots[k])
                 if slot is None:
                     break
                 queue.popleft()
                 running[slot] = (req, k)
+
+        while i < len(trace) or queue or running:
+            intake()
+            admit()
             if not running:
                 if queue:
                     raise MemoryError(f"job {queue[0][0].job_id}: a shot does not fit the arena")
@@ -113,7 +120,11 @@ class RTMServer:
                         dev_clock = max(dev_clock, trace[i].arrival)
                 continue
             max_active = max(max_active, len(running))
-            eng.step()
+            eng.launch()
+            if realtime:  # requests arriving during the replay upload while it runs
+                intake()
+                admit()
+            eng.wait()
             busy_ms += eng.last_ms
             pts += eng.last_points
             dev_clock += eng.last_ms / 1e3

@@ -194,8 +194,13 @@ unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d);
 unsigned long long w2d_batch_free_bytes(w2d_batch* b);
 /* Admit a shot; W2D_ENOMEM when it does not fit now (retry after a fetch). */
 int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out);
-/* Replay the captured time loop once over all active shots. */
+/* Replay the captured time loop once over all active shots (launch + wait). */
 int w2d_batch_step(w2d_batch* b, int* n_finished);
+/* The two halves of w2d_batch_step: launch returns at once (shots submitted while
+ * a replay is in flight upload on a second stream and join the next launch);
+ * wait finishes the replay and retires shots that reached the end. */
+int w2d_batch_launch(w2d_batch* b);
+int w2d_batch_wait(w2d_batch* b, int* n_finished);
 /* 1 finished, 0 running, -1 unused slot. */
 int w2d_batch_is_finished(w2d_batch* b, int slot);
 /* Copy a finished shot's image and illumination (nz, nx) out and free its memory. */
