@@ -69,6 +69,13 @@ _SIGS = {
                                 c_int, c_void_p]),
     "w2d_fwi_gradient": (c_int, [c_void_p, c_void_p, c_void_p]),
     "w2d_engine_synchronize": (c_int, [c_void_p]),
+    "w2d_elastic_create": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_float, c_float,
+                                   ctypes.c_double, c_int, c_float, c_int]),
+    "w2d_elastic_destroy": (None, [c_void_p]),
+    "w2d_elastic_forward": (c_int, [c_void_p] * 6 + [c_int, c_int, c_int, c_void_p, c_int, c_int,
+                                                      c_void_p]),
+    "w2d_elastic_gradient": (c_int, [c_void_p] * 6),
+    "w2d_elastic_last_ms": (c_float, [c_void_p]),
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),

@@ -44,8 +44,8 @@ struct BShot {
     unsigned* done;     // per tile: phase steps completed
 };
 
-// TMA descriptors of one shot (global memory, 64-byte aligned).
-struct alignas(64) BMaps {
+// TMA descriptors of one shot (global memory; CUtensorMap carries its own alignment).
+struct BMaps {
     CUtensorMap curr[6];
     CUtensorMap prev[6];
     CUtensorMap vel[2];

@@ -1,0 +1,183 @@
+// elastic_adjoint_kernels.cuh -- elastic modelling pieces and the exact discrete
+// adjoint of the velocity-stress step (parameter gradients for elastic RTM).
+//
+// Modelling (no counterpart in the reference, which only exports the step):
+//   * state u_n = (vx, vz, sxx, szz, sxz); the step is elastic_kernels.cuh
+//     (wave2d.c:95-212), updated cells M = rows [1 if free surface else 2, nz-2),
+//     columns [2, nx-2); every other cell stays zero (zero start, sources and
+//     receivers on M), so the free-surface rule reduces to zero stresses on row 0;
+//   * vertical force source: vz[src] += w[n] * dt before step n;
+//   * vertical-strain receivers: d_n = Dz- vz of u_{n+1} at (rec_iz, rec_ix),
+//     the same 4th-order staggered difference the stress update uses.
+//
+// Adjoint of one step u' = S(V(u)) (V: v' = s(v + dt b G sigma); S: sigma' =
+// s(sigma + dt C E v')), with the staggered operators' transposes
+// D-^T = -D+ and D+^T = -D- on fields that vanish outside M:
+//   K1  q = s * adj_sigma'                 (adjoint stress after S^T)
+//       t = dt * C q                       (per cell, C = [[l+2m, l, 0],[l, l+2m, 0],[0,0,m]])
+//   K2  adj_v += E^T t = -(Dx+ txx + Dz- txz,  Dz+ tzz + Dx- txz)
+//       g_lambda += dt (exx + ezz)(qxx + qzz),  g_mu += dt (2 exx qxx + 2 ezz qzz + exz qxz),
+//       with the forward strains e = E v_{n+1}
+//   K3  g_bx += s dt adj_vx (Dx+ sxx_n + Dz- sxz_n), g_bz likewise (forward stresses of u_n);
+//       adj_v = s adj_v;  r = dt b adj_v
+//   K4  adj_sigma = q + G^T r = q - (Dx- rx,  Dz- rz,  Dz+ rx + Dx+ rz)
+// Receiver residuals enter as adj_vz += Dz-^T (residual) on the four cells of
+// the receiver's stencil.  Float32; not bit-for-bit with anything, checked
+// against finite differences.
+#pragma once
+
+#include "elastic_kernels.cuh"
+
+namespace w2d {
+
+struct ElState {
+    float *vx, *vz, *sxx, *szz, *sxz;
+};
+
+struct ElParams {
+    const float *lam, *mu, *bx, *bz;
+    const float* sponge;  // pitched, or null
+};
+
+__device__ __forceinline__ bool el_in_m(int ix, int iz, int nx, int nz, int fs)
+{
+    return iz >= (fs ? 1 : 2) && iz < nz - 2 && ix >= 2 && ix < nx - 2;
+}
+
+// reads a[iz*L+ix] with zero outside the grid (rows/cols outside M hold zero)
+__device__ __forceinline__ float el_at(const float* a, int ix, int iz, int nx, int nz, int L)
+{
+    return (ix >= 0 && ix < nx && iz >= 0 && iz < nz) ? a[(size_t)iz * L + ix] : 0.0f;
+}
+
+// c1*(a[+1]-a[0]) + c2*(a[+2]-a[-1]) along x or z
+__device__ __forceinline__ float d_fwd_x(const float* a, int ix, int iz, int nx, int nz, int L)
+{
+    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    return k1 * (el_at(a, ix + 1, iz, nx, nz, L) - el_at(a, ix, iz, nx, nz, L)) +
+           k2 * (el_at(a, ix + 2, iz, nx, nz, L) - el_at(a, ix - 1, iz, nx, nz, L));
+}
+__device__ __forceinline__ float d_bwd_x(const float* a, int ix, int iz, int nx, int nz, int L)
+{
+    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    return k1 * (el_at(a, ix, iz, nx, nz, L) - el_at(a, ix - 1, iz, nx, nz, L)) +
+           k2 * (el_at(a, ix + 1, iz, nx, nz, L) - el_at(a, ix - 2, iz, nx, nz, L));
+}
+__device__ __forceinline__ float d_fwd_z(const float* a, int ix, int iz, int nx, int nz, int L)
+{
+    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    return k1 * (el_at(a, ix, iz + 1, nx, nz, L) - el_at(a, ix, iz, nx, nz, L)) +
+           k2 * (el_at(a, ix, iz + 2, nx, nz, L) - el_at(a, ix, iz - 1, nx, nz, L));
+}
+__device__ __forceinline__ float d_bwd_z(const float* a, int ix, int iz, int nx, int nz, int L)
+{
+    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    return k1 * (el_at(a, ix, iz, nx, nz, L) - el_at(a, ix, iz - 1, nx, nz, L)) +
+           k2 * (el_at(a, ix, iz + 1, nx, nz, L) - el_at(a, ix, iz - 2, nx, nz, L));
+}
+
+#define EL_CELL                                                  \
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;        \
+    const int iz = blockIdx.y * blockDim.y + threadIdx.y;        \
+    if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) return;    \
+    const int L = g.ldx;                                         \
+    const size_t c = (size_t)iz * L + ix;                        \
+    const float sp = p.sponge ? p.sponge[c] : 1.0f;
+
+// K1
+static __global__ void el_adj_k1(ElGeom g, ElParams p, ElState a, ElState t)
+{
+    EL_CELL
+    const float qxx = sp * a.sxx[c], qzz = sp * a.szz[c], qxz = sp * a.sxz[c];
+    a.sxx[c] = qxx;
+    a.szz[c] = qzz;
+    a.sxz[c] = qxz;
+    const float l = p.lam[c], m = p.mu[c];
+    t.sxx[c] = g.dt * ((l + 2.0f * m) * qxx + l * qzz);
+    t.szz[c] = g.dt * (l * qxx + (l + 2.0f * m) * qzz);
+    t.sxz[c] = g.dt * m * qxz;
+}
+
+// K2 (fwd: forward velocities of u_{n+1})
+static __global__ void el_adj_k2(ElGeom g, ElParams p, ElState a, ElState t, ElState fwd,
+                                 float* g_lam, float* g_mu)
+{
+    EL_CELL
+    (void)sp;
+    const int nx = g.nx, nz = g.nz;
+    a.vx[c] -= d_fwd_x(t.sxx, ix, iz, nx, nz, L) * g.rdx + d_bwd_z(t.sxz, ix, iz, nx, nz, L) * g.rdz;
+    a.vz[c] -= d_fwd_z(t.szz, ix, iz, nx, nz, L) * g.rdz + d_bwd_x(t.sxz, ix, iz, nx, nz, L) * g.rdx;
+    const float exx = d_bwd_x(fwd.vx, ix, iz, nx, nz, L) * g.rdx;
+    const float ezz = d_bwd_z(fwd.vz, ix, iz, nx, nz, L) * g.rdz;
+    const float exz = d_fwd_x(fwd.vz, ix, iz, nx, nz, L) * g.rdx +
+                      d_fwd_z(fwd.vx, ix, iz, nx, nz, L) * g.rdz;
+    const float qxx = a.sxx[c], qzz = a.szz[c], qxz = a.sxz[c];
+    g_lam[c] += g.dt * (exx + ezz) * (qxx + qzz);
+    g_mu[c] += g.dt * (2.0f * exx * qxx + 2.0f * ezz * qzz + exz * qxz);
+}
+
+// K3 (fwd: forward stresses of u_n)
+static __global__ void el_adj_k3(ElGeom g, ElParams p, ElState a, ElState r, ElState fwd,
+                                 float* g_bx, float* g_bz)
+{
+    EL_CELL
+    const int nx = g.nx, nz = g.nz;
+    const float gx = d_fwd_x(fwd.sxx, ix, iz, nx, nz, L) * g.rdx +
+                     d_bwd_z(fwd.sxz, ix, iz, nx, nz, L) * g.rdz;
+    const float gz = d_bwd_x(fwd.sxz, ix, iz, nx, nz, L) * g.rdx +
+                     d_fwd_z(fwd.szz, ix, iz, nx, nz, L) * g.rdz;
+    g_bx[c] += sp * g.dt * a.vx[c] * gx;
+    g_bz[c] += sp * g.dt * a.vz[c] * gz;
+    const float vx = sp * a.vx[c], vz = sp * a.vz[c];
+    a.vx[c] = vx;
+    a.vz[c] = vz;
+    r.vx[c] = g.dt * p.bx[c] * vx;
+    r.vz[c] = g.dt * p.bz[c] * vz;
+}
+
+// K4
+static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r)
+{
+    EL_CELL
+    (void)sp;
+    const int nx = g.nx, nz = g.nz;
+    a.sxx[c] -= d_bwd_x(r.vx, ix, iz, nx, nz, L) * g.rdx;
+    a.szz[c] -= d_bwd_z(r.vz, ix, iz, nx, nz, L) * g.rdz;
+    a.sxz[c] -= d_fwd_z(r.vx, ix, iz, nx, nz, L) * g.rdz + d_fwd_x(r.vz, ix, iz, nx, nz, L) * g.rdx;
+}
+
+// Forward pieces: source (vz += w * dt) and vertical-strain receivers of u_{n+1}.
+static __global__ void el_inject_kernel(float* vz, int ldx, int src_ix, int src_iz, const float* w,
+                                        float scale)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) vz[(size_t)src_iz * ldx + src_ix] += w[0] * scale;
+}
+
+static __global__ void el_sample_kernel(ElGeom g, const float* vz, const int* rec_ix, int n_rec,
+                                        int rec_iz, float* out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_rec) return;
+    out[k] = d_bwd_z(vz, rec_ix[k], rec_iz, g.nx, g.nz, g.ldx) * g.rdz;
+}
+
+// Adjoint of the sampling: adj_vz += Dz-^T (residual) at each receiver, i.e. on
+// rows rec_iz (+c1), rec_iz-1 (-c1), rec_iz+1 (+c2), rec_iz-2 (-c2), cells of M only.
+static __global__ void el_adj_receivers(ElGeom g, float* adj_vz, const int* rec_ix, int n_rec,
+                                        int rec_iz, const float* resid)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;  // serial: receivers may share cells
+    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    const int dz[4] = {0, -1, 1, -2};
+    const float cf[4] = {k1, -k1, k2, -k2};
+    for (int k = 0; k < n_rec; ++k) {
+        const float r = resid[k] * g.rdz;
+        for (int j = 0; j < 4; ++j) {
+            const int iz = rec_iz + dz[j], ix = rec_ix[k];
+            if (el_in_m(ix, iz, g.nx, g.nz, g.free_surface))
+                adj_vz[(size_t)iz * g.ldx + ix] += cf[j] * r;
+        }
+    }
+}
+
+}  // namespace w2d

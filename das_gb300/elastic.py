@@ -1,0 +1,101 @@
+"""Elastic (velocity-stress) modelling and its gradient on one GB300.
+
+The reference ships the elastic step (tsw_rtm/c_engine/wave2d.c:95-212) but no
+elastic time loop.  ``ElasticSolver2D`` runs that step (same arithmetic, same
+staggered grid, free surface and sponge) with a vertical force source and
+vertical-strain receivers -- the quantity a DAS fibre records -- and
+``ElasticModeling`` puts the hand-written adjoint behind torch.autograd, so the
+gradient of any loss on the traces with respect to lambda, mu and the
+buoyancies (and, through ``gardner_parameters``, with respect to the shear
+velocity) is available, the forward states being recomputed from checkpoints.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import normalize_index, normalize_indices
+
+
+class ElasticSolver2D:
+    def __init__(self, nx: int, nz: int, dx: float, dz: float, dt: float, n_sponge: int = 30,
+                 sponge_alpha: float = 0.0015, free_surface_top: bool = True):
+        self.nx, self.nz = nx, nz
+        self.dx, self.dz, self.dt = float(dx), float(dz), float(dt)
+        self.n_sponge, self.sponge_alpha = n_sponge, float(sponge_alpha)
+        self.free_surface_top = free_surface_top
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.w2d_elastic_create(ctypes.byref(h), nx, nz, self.dx, self.dz, self.dt,
+                                                n_sponge, self.sponge_alpha,
+                                                1 if free_surface_top else 0))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self._lib.w2d_elastic_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def last_ms(self) -> float:
+        return float(self._lib.w2d_elastic_last_ms(self._h))
+
+
+def gardner_parameters(vs: torch.Tensor, vp_over_vs: float = 1.73):
+    """(lambda, mu, buo_x, buo_z) from the shear velocity: vp = 1.73 vs, Gardner's
+    density rho = 310 vp^0.25 (kg/m^3, vp in m/s); differentiable in torch."""
+    vp = vp_over_vs * vs
+    rho = 310.0 * vp ** 0.25
+    mu = rho * vs * vs
+    lam = rho * vp * vp - 2.0 * mu
+    b = 1.0 / rho
+    return lam, mu, b, b
+
+
+class ElasticModeling(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, lam, mu, bx, bz, solver: ElasticSolver2D, wavelet, source_ix, source_iz,
+                receiver_ix, receiver_iz):
+        ps = [t.detach().to(torch.float32).contiguous() for t in (lam, mu, bx, bz)]
+        for t in ps:
+            if not t.is_cuda or tuple(t.shape) != (solver.nz, solver.nx):
+                raise ValueError("parameters must be CUDA tensors of shape (nz, nx)")
+        w = np.ascontiguousarray(wavelet, dtype=np.float32).reshape(-1)
+        rix = normalize_indices(receiver_ix, solver.nx, "receiver_ix")
+        six = normalize_index(source_ix, solver.nx, "source_ix")
+        siz = normalize_index(source_iz, solver.nz, "source_iz")
+        riz = normalize_index(receiver_iz, solver.nz, "receiver_iz")
+        traces = torch.empty((len(w), len(rix)), dtype=torch.float32, device=ps[0].device)
+        torch.cuda.current_stream(ps[0].device).synchronize()
+        _lib.check(solver._lib.w2d_elastic_forward(
+            solver._h, *[t.data_ptr() for t in ps], w.ctypes.data, len(w), six, siz,
+            rix.ctypes.data, len(rix), riz, traces.data_ptr()))
+        ctx.solver = solver
+        ctx.shape = tuple(ps[0].shape)
+        ctx.device = ps[0].device
+        return traces
+
+    @staticmethod
+    def backward(ctx, grad_traces):
+        g = grad_traces.detach().to(torch.float32).contiguous()
+        outs = [torch.empty(ctx.shape, dtype=torch.float32, device=ctx.device) for _ in range(4)]
+        torch.cuda.current_stream(ctx.device).synchronize()
+        _lib.check(ctx.solver._lib.w2d_elastic_gradient(ctx.solver._h, g.data_ptr(),
+                                                        *[o.data_ptr() for o in outs]))
+        return (*outs, None, None, None, None, None, None)
+
+
+def elastic_traces(vs: torch.Tensor, solver: ElasticSolver2D, wavelet, source_ix, source_iz,
+                   receiver_ix, receiver_iz=2):
+    """Vertical-strain traces (nt, n_rec) for a shear-velocity model; differentiable in vs."""
+    return ElasticModeling.apply(*gardner_parameters(vs), solver, wavelet, source_ix, source_iz,
+                                 receiver_ix, receiver_iz)

@@ -159,6 +159,26 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
 int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev);
 int w2d_engine_synchronize(w2d_engine* e);
 
+/* ---- Elastic modelling and gradient (no reference counterpart: the reference only
+ * exports the step, wave2d.c:95-212, which these calls advance) ----
+ * Vertical force source vz[src] += w[n]*dt before step n; vertical-strain
+ * receivers (Dz- vz after each step) at row rec_iz, columns in [2, nx-2); the
+ * Cerjan sponge of (n_sponge, alpha).  Parameters and outputs are DEVICE arrays,
+ * contiguous (nz, nx); wavelet and rec_ix are HOST arrays. */
+typedef struct w2d_elastic w2d_elastic;
+int w2d_elastic_create(w2d_elastic** out, int nx, int nz, float dx, float dz, double dt,
+                       int n_sponge, float sponge_alpha, int free_surface_top);
+void w2d_elastic_destroy(w2d_elastic* e);
+int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const float* bx,
+                        const float* bz, const float* wavelet, int nt, int src_ix, int src_iz,
+                        const int* rec_ix, int n_rec, int rec_iz, float* traces_dev);
+/* Gradients of sum(resid * traces) with respect to lambda, mu, buo_x, buo_z (any
+ * output may be NULL); exact adjoint of the discrete step, forward states
+ * recomputed from checkpoints. */
+int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
+                         float* g_bx, float* g_bz);
+float w2d_elastic_last_ms(w2d_elastic* e);
+
 /* ---- Part 3: batched / continuously fed migration (no reference counterpart:
  * the reference migrates shots one after another, rtm_engine.py:125-143) ----- */
 

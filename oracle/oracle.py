@@ -331,3 +331,48 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     if nb == 0.0:
         return 0.0 if na == 0.0 else float("inf")
     return float(na / nb)
+
+
+# --------------------------------------------------------------------------- elastic loop
+
+def elastic_forward(g: Grid, lam, mu, bx, bz, source_ts, source_ix, source_iz, receiver_ix,
+                    receiver_iz, precision="f32"):
+    """Elastic modelling around the reference step (wave2d.c:95-212), which has no time
+    loop of its own in the reference: before step n, vz[src] += w[n] * dt; after it,
+    the vertical strain Dz- vz (4th-order staggered, the stress update's operator)
+    is sampled at (receiver_iz, receiver_ix).  Row -1 reads zero."""
+    dt_ = _dtype(precision)
+    nz, nx = g.nz, g.nx
+    f = [np.zeros((nz, nx), dtype=dt_) for _ in range(5)]
+    vx, vz, sxx, szz, sxz = f
+    P = [np.ascontiguousarray(a, dtype=dt_) for a in (lam, mu, bx, bz)]
+    sp = g.sponge().astype(dt_)
+    w = np.asarray(source_ts, dtype=np.float32).astype(dt_)
+    dtv = dt_(g.dt) if precision == "f32" else g.dt
+    rix = np.asarray(receiver_ix, dtype=np.int64)
+    k1, k2 = dt_(9.0 / 8.0), dt_(-1.0 / 24.0)
+    rdz = dt_(1.0) / dt_(g.dz)
+    out = np.zeros((len(w), len(rix)), dtype=dt_)
+    r = receiver_iz
+
+    def row(a, i):
+        return a[i] if i >= 0 else np.zeros(nx, dtype=dt_)
+
+    for n in range(len(w)):
+        vz[source_iz, source_ix] += w[n] * dtv
+        elastic_step(vx, vz, sxx, szz, sxz, *P, sp, nx, nz, g.dx, g.dz, g.dt, g.free_surface_top,
+                     precision)
+        d = k1 * (row(vz, r) - row(vz, r - 1)) + k2 * (row(vz, r + 1) - row(vz, r - 2))
+        out[n] = d[rix] * rdz
+    return out
+
+
+def gardner_parameters(vs, vp_over_vs=1.73, precision="f64"):
+    dt_ = _dtype(precision)
+    vs = np.asarray(vs, dtype=dt_)
+    vp = dt_(vp_over_vs) * vs
+    rho = dt_(310.0) * vp ** dt_(0.25)
+    mu = rho * vs * vs
+    lam = rho * vp * vp - dt_(2.0) * mu
+    b = dt_(1.0) / rho
+    return lam, mu, b, b
