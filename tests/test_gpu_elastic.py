@@ -29,6 +29,10 @@ def _setup():
     from das_gb300.elastic import ElasticSolver2D
     from das_gb300.wave_solver import ricker_wavelet
     w, _ = ricker_wavelet(12.0, DT, 0.15)
+    # a unit force gives strains of ~1e-12 here, whose products with the adjoint
+    # fields fall below float32's normal range; the modelling is linear in the
+    # source, so scale it
+    w = (w * 1e6).astype(np.float32)
     rix = np.arange(4, NX - 4)
     grid = o.Grid(NX, NZ, DX, DX, DT, 10, 0.003, True)
     solver = ElasticSolver2D(NX, NZ, DX, DX, DT, n_sponge=10, sponge_alpha=0.003)
@@ -48,14 +52,16 @@ def test_elastic_traces_match_oracle_loop():
 
 
 def test_elastic_gradient_matches_finite_differences():
+    """dJ/dvs for J = sum(R * d(vs)) with fixed random weights R: the adjoint applied
+    to R, compared with central differences of the float64 oracle (a misfit whose
+    residual sat at float32 rounding level would test rounding, not the adjoint)."""
     from das_gb300.elastic import elastic_traces
     torch, solver, grid, w, rix = _setup()
-    vs, vs_true = _model()
-    d_obs = o.elastic_forward(grid, *o.gardner_parameters(vs_true), w, 40, 3, rix, 2,
-                              precision="f64")
+    vs, _ = _model()
+    R = np.random.default_rng(9).standard_normal((len(w), len(rix))).astype(np.float32)
     v = torch.tensor(vs, device="cuda", requires_grad=True)
     d = elastic_traces(v, solver, w, 40, 3, rix, 2)
-    J = 0.5 * torch.sum((d - torch.tensor(d_obs.astype(np.float32), device="cuda")) ** 2)
+    J = torch.sum(d * torch.tensor(R, device="cuda"))
     J.backward()
     g = v.grad.cpu().numpy()
     assert np.isfinite(g).all() and np.abs(g).max() > 0
@@ -63,10 +69,10 @@ def test_elastic_gradient_matches_finite_differences():
     def J64(vs64):
         dd = o.elastic_forward(grid, *o.gardner_parameters(vs64), w, 40, 3, rix, 2,
                                precision="f64")
-        return 0.5 * np.sum((dd - d_obs) ** 2)
+        return float(np.sum(dd * R))
 
     rng = np.random.default_rng(4)
-    cells = [(int(rng.integers(6, 30)), int(rng.integers(14, 66))) for _ in range(16)]
+    cells = [(int(rng.integers(1, 30)), int(rng.integers(14, 66))) for _ in range(16)]
     fd, an = [], []
     for iz, ix in cells:
         h = 1e-3 * float(vs[iz, ix])
@@ -79,4 +85,6 @@ def test_elastic_gradient_matches_finite_differences():
     fd, an = np.array(fd), np.array(an)
     err = np.linalg.norm(an - fd) / np.linalg.norm(fd)
     print(f"elastic gradient vs central differences on 16 cells: rel-L2 {err:.2e}")
-    assert err < 2e-2, (an, fd)
+    for (iz, ix), a, f in zip(cells, an, fd):
+        print(f"  cell ({iz},{ix}) adjoint {a:+.5e} finite-difference {f:+.5e}")
+    assert err < 2e-2
