@@ -446,15 +446,79 @@ def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
         v = gaussian_filter(v, 3.0).astype(np.float32)
         dt = 5e-4
         w, _ = ricker_wavelet(float(rng.uniform(3.0, 5.0)), dt, nt * dt)
+        n_sh = int(rng.integers(1, 33))
+        if kind == "elastic":
+            # shear velocity from the same model; vertical-strain observations
+            vs = (v / 1.73).astype(np.float32)  # vp = 1.73 vs = v: same CFL as the acoustic
+            dte, nte = dt, nt
+            we, _ = ricker_wavelet(float(rng.uniform(3.0, 5.0)), dte, nte * dte)
+            we = (we * 1e6).astype(np.float32)
+            rix = np.arange(2, nx - 2)
+            data = (rng.standard_normal((nte, len(rix))) * 1e-3).astype(np.float32)
+            shots = [ShotJob(nx, nz, d, d, dte, vs, vs, we, data, rix,
+                             int(2 + (k + 0.5) * (nx - 4) / n_sh), 2, 2, 2, 30, 0.0015, True)
+                     for k in range(n_sh)]
+            return kind, shots
         rix = np.arange(nx)
         data = (rng.standard_normal((nt, nx)) * 1e-8).astype(np.float32)
-        n_sh = int(rng.integers(1, 33))
         shots = [ShotJob(nx, nz, d, d, dt, v, v, w, data, rix,
                          int((k + 0.5) * nx / n_sh), 2, 2, 2, 30, 0.0015, True)
                  for k in range(n_sh)]
         return kind, shots
 
     return poisson_trace(n_jobs, rate, make, seed=seed)
+
+
+def run_elastic(args, dist):
+    """Elastic gradient workload: 1024 x 2048 grid, dx 2 m, free surface, vs 300 -> 1200 m/s
+    with a 20 m low-velocity zone dipping 70 degrees, vp = 1.73 vs, Gardner density; 5 Hz
+    Ricker, dt 0.2 ms, nt 6000; vertical-strain receivers on every interior column; per
+    step one shot's forward modelling + adjoint gradient through torch.autograd."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+    from das_gb300.elastic import ElasticSolver2D, elastic_traces
+    from das_gb300.synthetic import elastic_fault_zone
+    from das_gb300.wave_solver import ricker_wavelet
+    nz, nx, d, dt = 1024, 2048, 2.0, 2e-4
+    nt = args.el_nt
+    vs_true = elastic_fault_zone(nz, nx, d)
+    vs_mig = gaussian_filter(vs_true.astype(np.float64), 5.0).astype(np.float32)
+    w, _ = ricker_wavelet(5.0, dt, nt * dt)
+    w = (w * 1e6).astype(np.float32)
+    rix = np.arange(2, nx - 2)
+    solver = ElasticSolver2D(nx, nz, d, d, dt, n_sponge=40, sponge_alpha=0.0015)
+    src = [int(s) for s in np.linspace(40, nx - 41, 64).astype(int)]
+    K, W = args.steps, 1
+    vt = torch.tensor(vs_true, device="cuda")
+    obs = []
+    for k in range(K + W):
+        with torch.no_grad():
+            obs.append(elastic_traces(vt, solver, w, src[k * 7 % 64], 2, rix, 2).clone())
+    times = []
+    fwd_ms, grad_ms = [], []
+    for k in range(K + W):
+        v = torch.tensor(vs_mig, device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dd = elastic_traces(v, solver, w, src[k * 7 % 64], 2, rix, 2)
+        f_ms = solver.last_ms
+        J = 0.5 * torch.sum((dd - obs[k]) ** 2)
+        J.backward()
+        torch.cuda.synchronize()
+        if k >= W:
+            times.append(time.perf_counter() - t0)
+            fwd_ms.append(f_ms)
+            grad_ms.append(solver.last_ms)
+    pts = 2.0 * nz * nx * nt
+    out = {"metric": "elastic RTM gradient Gpts/s", "value": pts * K / sum(times) / 1e9,
+           "unit": "Gpts/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+           "data": "synthetic", "steps": K, "warmup": W,
+           "config": {"workload": f"elastic velocity-stress gradient 1024x2048, dx 2 m, nt {nt}, "
+                                  f"{len(rix)} vertical-strain receivers, 5 Hz, checkpointed"},
+           "s_per_shot": sum(times) / K, "device_ms_forward": statistics.mean(fwd_ms),
+           "device_ms_gradient": statistics.mean(grad_ms),
+           "counted_points_per_shot": pts}
+    print(json.dumps(out), flush=True)
 
 
 def run_served(args, dist):
@@ -470,8 +534,10 @@ def run_served(args, dist):
     tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
     eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=4096, tile=tile,
                       steps_per_launch=args.spl, launches_per_graph=args.lpg)
-    eng.run(trace[0].shots[:1])  # graph capture, first touch
-    out, st = RTMServer(eng).serve(trace, realtime=True)
+    from das_gb300.elastic import ElasticExecutor
+    eng.run([s for r in trace if r.kind == "acoustic" for s in r.shots][:1])  # graph capture
+    ex = ElasticExecutor()
+    out, st = RTMServer(eng, elastic_executor=ex).serve(trace, realtime=True)
     eng.close()
     # plain per-shot loop over the first jobs of the same trace, arrivals on the wall clock
     m = min(args.plain_jobs, len(trace))
@@ -482,14 +548,22 @@ def run_served(args, dist):
         if wait > 0:
             time.sleep(wait)
         j0 = r.shots[0]
-        s = WaveSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha, True)
-        e = TSWRTMEngine(s, "all")
-        fm = FloodModels(j0.vel_fwd, j0.vel_fwd, j0.vel_bwd, 0, 0)
-        for j in r.shots:
-            e.migrate_shot(fm, j.wavelet, j.source_ix, j.source_iz, j.data, j.receiver_ix, 2, 2)
-            shots_done += 1
-        s.close()
+        if r.kind == "elastic":
+            es = ex._solver(j0)
+            for j in r.shots:
+                ex.migrate_shot(es, j)
+                shots_done += 1
+        else:
+            s = WaveSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha, True)
+            e = TSWRTMEngine(s, "all")
+            fm = FloodModels(j0.vel_fwd, j0.vel_fwd, j0.vel_bwd, 0, 0)
+            for j in r.shots:
+                e.migrate_shot(fm, j.wavelet, j.source_ix, j.source_iz, j.data, j.receiver_ix, 2,
+                               2)
+                shots_done += 1
+            s.close()
         lat.append(time.perf_counter() - t0 - r.arrival)
+    ex.close()
     plain_span = time.perf_counter() - t0
     plain = {"jobs": m, "shots": shots_done, "shots_per_s": shots_done / plain_span,
              "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
@@ -512,7 +586,9 @@ def run_served(args, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", default="large", choices=["large", "batched", "served"])
+    ap.add_argument("--workload", default="large",
+                    choices=["large", "batched", "served", "elastic"])
+    ap.add_argument("--el-nt", type=int, default=6000)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)
@@ -555,6 +631,8 @@ def main():
             run_batched(args, dist)
         elif args.workload == "served":
             run_served(args, dist)
+        elif args.workload == "elastic":
+            run_elastic(args, dist)
         else:
             run_ours(args, dist)
     finally:

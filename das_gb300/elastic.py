@@ -99,3 +99,68 @@ def elastic_traces(vs: torch.Tensor, solver: ElasticSolver2D, wavelet, source_ix
     """Vertical-strain traces (nt, n_rec) for a shear-velocity model; differentiable in vs."""
     return ElasticModeling.apply(*gardner_parameters(vs), solver, wavelet, source_ix, source_iz,
                                  receiver_ix, receiver_iz)
+
+
+class ElasticExecutor:
+    """Runs elastic migration jobs on a worker thread with its own CUDA stream, so
+    they overlap the acoustic batch on the device.  A job's shots carry the shear
+    velocity in ``vel_fwd`` and observed vertical-strain traces in ``data``; each
+    shot's result is (dJ/dvs, None) for J = 0.5 * ||d(vs) - data||^2."""
+
+    def __init__(self):
+        import queue
+        import threading
+        self._q = queue.Queue()
+        self._done = []
+        self._lock = threading.Lock()
+        self._pending = 0
+        self._solvers = {}
+        self._t = threading.Thread(target=self._loop, daemon=True)
+        self._t.start()
+
+    def _solver(self, s):
+        key = (s.nx, s.nz, s.dx, s.dz, s.dt, s.n_sponge, s.sponge_alpha, s.free_surface_top)
+        if key not in self._solvers:
+            self._solvers[key] = ElasticSolver2D(s.nx, s.nz, s.dx, s.dz, s.dt, s.n_sponge,
+                                                 s.sponge_alpha, s.free_surface_top)
+        return self._solvers[key]
+
+    @staticmethod
+    def migrate_shot(solver, shot):
+        vs = torch.tensor(np.asarray(shot.vel_fwd, np.float32), device="cuda", requires_grad=True)
+        d = elastic_traces(vs, solver, shot.wavelet, shot.source_ix, shot.source_iz,
+                           shot.receiver_ix, shot.receiver_iz)
+        obs = torch.tensor(np.asarray(shot.data, np.float32), device="cuda")
+        J = 0.5 * torch.sum((d - obs) ** 2)
+        J.backward()
+        return vs.grad.detach().cpu().numpy(), None
+
+    def _loop(self):
+        import time
+        torch.cuda.set_stream(torch.cuda.Stream())
+        while True:
+            req = self._q.get()
+            if req is None:
+                return
+            res = [self.migrate_shot(self._solver(s), s) for s in req.shots]
+            with self._lock:
+                self._done.append((req.job_id, res, time.perf_counter()))
+                self._pending -= 1
+
+    def submit(self, req):
+        with self._lock:
+            self._pending += 1
+        self._q.put(req)
+
+    def pending(self) -> int:
+        with self._lock:
+            return self._pending
+
+    def poll(self):
+        with self._lock:
+            out, self._done = self._done, []
+        return out
+
+    def close(self):
+        self._q.put(None)
+        self._t.join()

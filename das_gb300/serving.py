@@ -89,10 +89,7 @@ class RTMServer:
                                                     [None] * len(req.shots))
                 remaining[req.job_id] = len(req.shots)
                 if req.kind == "elastic" and self.elastic_executor is not None:
-                    res = self.elastic_executor(req)
-                    responses[req.job_id].results = list(res)
-                    remaining[req.job_id] = 0
-                    responses[req.job_id].finished = now()
+                    self.elastic_executor.submit(req)
                 else:
                     for k in range(len(req.shots)):
                         queue.append((req, k))
@@ -107,9 +104,26 @@ class RTMServer:
                 queue.popleft()
                 running[slot] = (req, k)
 
-        while i < len(trace) or queue or running:
+        ex = self.elastic_executor
+
+        def collect_elastic():
+            nonlocal n_shots
+            if ex is None:
+                return
+            for job_id, res, t_done in ex.poll():
+                responses[job_id].results = list(res)
+                responses[job_id].finished = t_done - t_start if realtime else dev_clock
+                n_shots += len(res)
+                remaining[job_id] = 0
+
+        while i < len(trace) or queue or running or (ex is not None and ex.pending()):
             intake()
             admit()
+            collect_elastic()
+            if not running and not queue and ex is not None and ex.pending() and (
+                    i >= len(trace) or trace[i].arrival > now()):
+                time.sleep(0.002)  # only elastic work in flight
+                continue
             if not running:
                 if queue:
                     raise MemoryError(f"job {queue[0][0].job_id}: a shot does not fit the arena")

@@ -145,3 +145,19 @@ def batched_gathers(n: int = 256, seed: int = 0, dt: float = 5e-4, nt_range=(150
         w, _ = ricker_wavelet(f0, dt, nt * dt)
         out.append(Gather(nz, nx, d, dt, len(w), f0, v, int(rng.integers(40, nx - 40)), w))
     return out
+
+
+def elastic_fault_zone(nz: int = 1024, nx: int = 2048, dx: float = 2.0, vs_top: float = 300.0,
+                       vs_bottom: float = 1200.0, zone_width_m: float = 20.0, dip_deg: float = 70.0,
+                       zone_factor: float = 0.7) -> np.ndarray:
+    """Shear velocity rising linearly with depth, cut by a low-velocity fault zone of
+    the given width dipping at dip_deg from the middle of the surface."""
+    z = (np.arange(nz) * dx)[:, None]
+    x = (np.arange(nx) * dx)[None, :]
+    vs = vs_top + (vs_bottom - vs_top) * z / ((nz - 1) * dx) + 0.0 * x
+    x0 = 0.5 * (nx - 1) * dx
+    # distance to the plane through (x0, 0) dipping dip_deg
+    th = np.deg2rad(dip_deg)
+    dist = np.abs((x - x0) * np.sin(th) - z * np.cos(th))
+    vs = np.where(dist <= 0.5 * zone_width_m, vs * zone_factor, vs)
+    return vs.astype(np.float32)

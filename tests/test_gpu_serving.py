@@ -33,6 +33,45 @@ def _alone(job):
                                                job.source_iz, job.data, job.receiver_ix, 2, 2)
 
 
+def test_served_mix_with_elastic_jobs():
+    """Elastic jobs run on the executor's own stream while acoustic shots batch; each
+    result equals the same computation alone."""
+    import torch
+    from das_gb300.batch import BatchEngine, ShotJob
+    from das_gb300.elastic import ElasticExecutor, ElasticSolver2D
+    from das_gb300.serving import RTMRequest, RTMServer
+    from das_gb300.wave_solver import ricker_wavelet
+    rng = np.random.default_rng(5)
+    nz, nx, dt = 40, 96, 5e-4
+    vs = (300.0 + 600.0 * np.arange(nz)[:, None] / nz + 0.0 * np.arange(nx)[None, :]).astype(
+        np.float32)
+    w, _ = ricker_wavelet(12.0, dt, 0.05)
+    w = (w * 1e6).astype(np.float32)
+    rix = np.arange(2, nx - 2)
+    el_shots = [ShotJob(nx, nz, 5.0, 5.0, dt, vs, vs, w,
+                        (rng.standard_normal((len(w), len(rix))) * 1e-3).astype(np.float32), rix,
+                        s, 2, 2, 2, 10, 0.003, True) for s in (20, 60)]
+    trace = [RTMRequest(0, [_shot(rng, 50, 150, 80)], 0.0),
+             RTMRequest(1, el_shots, 0.0, kind="elastic"),
+             RTMRequest(2, [_shot(rng, 60, 120, 90), _shot(rng, 60, 120, 70)], 0.001)]
+    ex = ElasticExecutor()
+    eng = BatchEngine(arena_bytes=1 << 28, max_shots=8, tile=(4, 4), steps_per_launch=8,
+                      launches_per_graph=2)
+    out, stats = RTMServer(eng, elastic_executor=ex).serve(trace, realtime=True)
+    ex.close()
+    assert stats["shots"] == 5 and all(np.isfinite(r.latency) for r in out)
+    solver = ElasticSolver2D(nx, nz, 5.0, 5.0, dt, 10, 0.003, True)
+    for shot, (g, _) in zip(el_shots, out[1].results):
+        g_alone, _ = ElasticExecutor.migrate_shot(solver, shot)
+        np.testing.assert_array_equal(g, g_alone)
+        assert np.abs(g).max() > 0
+    for req in (trace[0], trace[2]):
+        for shot, (img, ill) in zip(req.shots, out[req.job_id].results):
+            ref_img, ref_ill = _alone(shot)
+            np.testing.assert_array_equal(img, ref_img)
+    del torch
+
+
 def test_served_results_equal_alone():
     from das_gb300.batch import BatchEngine
     from das_gb300.serving import RTMRequest, RTMServer
