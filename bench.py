@@ -238,6 +238,7 @@ def run_ours(args, dist):
     solver = WaveSolver2D(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
     if args.tile:
         solver.tile = tuple(int(t) for t in args.tile.split(","))
+    solver.l2_hints = bool(args.l2_hints)
     eng = solver._eng()
     K, W = args.steps, args.warmup
     n_sh = K + W
@@ -589,6 +590,7 @@ def main():
     ap.add_argument("--workload", default="large",
                     choices=["large", "batched", "served", "elastic"])
     ap.add_argument("--el-nt", type=int, default=6000)
+    ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)

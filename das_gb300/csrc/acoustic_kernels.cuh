@@ -47,6 +47,8 @@ struct AcGeom {
     const int* rec_ptr;       // CSR over columns: receivers of column ix are
     const int* rec_list;      //   rec_list[rec_ptr[ix] .. rec_ptr[ix+1])
     const int* shot;          // device ints {src_ix, src_iz, rec_iz}
+    int l2_hints;             // 1: keep p_curr, vel^2 dt^2 and p_next in L2 (evict-last),
+                              //    stream p_prev (evict-first)
 };
 
 // Per-launch pointers (all optional ones may be null).
@@ -114,13 +116,22 @@ __device__ __forceinline__ int sponge_dist(int ix, int iz, int nx, int nz, int n
 // Issue the TMA boxes of a tile at (x0, z0) onto `bar` (one elected thread).
 template <int WARPS, int RPW, int SPONGE>
 __device__ __forceinline__ void ac_issue_loads(float* smem, const AcMaps* m, int x0, int z0,
-                                               uint64_t* bar)
+                                               uint64_t* bar, int l2_hints = 0)
 {
     using T = AcTile<WARPS, RPW, SPONGE>;
     mbar_expect_tx(bar, T::TX_BYTES);
-    tma_load_2d(smem, &m->curr, x0 - AC_HX, z0 - 2, bar);
-    tma_load_2d(smem + T::C_FLOATS, &m->prev, x0, z0, bar);
-    tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar);
+    if (l2_hints) {
+        // p_curr is re-read next step as p_prev and vel^2 dt^2 every step; p_prev's
+        // plane is overwritten next step
+        const uint64_t keep = policy_evict_last(), drop = policy_evict_first();
+        tma_load_2d_hint(smem, &m->curr, x0 - AC_HX, z0 - 2, bar, keep);
+        tma_load_2d_hint(smem + T::C_FLOATS, &m->prev, x0, z0, bar, drop);
+        tma_load_2d_hint(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar, keep);
+    } else {
+        tma_load_2d(smem, &m->curr, x0 - AC_HX, z0 - 2, bar);
+        tma_load_2d(smem + T::C_FLOATS, &m->prev, x0, z0, bar);
+        tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar);
+    }
     if (SPONGE == SPONGE_ARRAY)
         tma_load_2d(smem + T::C_FLOATS + 2 * T::P_FLOATS, &m->sponge, x0, z0, bar);
 }
@@ -252,7 +263,10 @@ __device__ __forceinline__ void ac_tile_body(const float* smem, const AcGeom& g,
                 u[3] = fmul(u[3], sp.w);
             }
             const size_t off = (size_t)(zr0 + r) * ldx + ixb;
-            *reinterpret_cast<float4*>(s.p_next + off) = make_float4(u[0], u[1], u[2], u[3]);
+            if (g.l2_hints)  // read next step as p_curr
+                st_hint_v4(s.p_next + off, make_float4(u[0], u[1], u[2], u[3]), policy_evict_last());
+            else
+                *reinterpret_cast<float4*>(s.p_next + off) = make_float4(u[0], u[1], u[2], u[3]);
             if (fused) ac_fused_row(s, off, w2);
             w0 = w1;
             w1 = w2;
@@ -374,7 +388,7 @@ __global__ void __launch_bounds__(WARPS * 32)
         prefetch_tensormap(&maps.curr);
         mbar_init(bar, 1);
         fence_mbar_init();
-        ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar);
+        ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     }
     __syncthreads();
     if (!mbar_wait_bounded(bar, 0)) {

@@ -92,6 +92,7 @@ struct w2d_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     TileShape tile{4, 4};
+    int l2_hints = 0;
 
     int n_sponge = 0;
     DevBuf<float> sponge_lut, sponge_arr;
@@ -202,6 +203,7 @@ AcGeom geom(w2d_engine* e)
     g.rec_ptr = e->rec_ptr.p;
     g.rec_list = e->rec_list.p;
     g.shot = e->shot.p;
+    g.l2_hints = e->l2_hints;
     return g;
 }
 
@@ -507,6 +509,13 @@ int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
     W2D_CHECK_ARG(tile_supported(warps, rows_per_warp), "unsupported tile shape");
     e->tile = TileShape{warps, rows_per_warp};
     return ensure_tensor_maps(e);
+}
+
+int w2d_engine_set_l2_hints(w2d_engine* e, int on)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    e->l2_hints = on ? 1 : 0;
+    return W2D_OK;
 }
 
 int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes)

@@ -150,6 +150,7 @@ class RTMServer:
                 remaining[req.job_id] -= 1
                 if remaining[req.job_id] == 0:
                     responses[req.job_id].finished = now()
+        collect_elastic()  # results that completed after the loop's last check
         makespan = now()
         out = [responses[r.job_id] for r in trace]
         lat = [r.latency for r in out]

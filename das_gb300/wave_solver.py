@@ -63,6 +63,7 @@ class WaveSolver2D:
         self._engine_sponge = None
         self.storage = "auto"
         self.tile = None  # (warps, rows_per_warp) or None for the default
+        self.l2_hints = False  # L2 residency hints in the step kernel
 
     # -- engine handle -----------------------------------------------------------
     def _eng(self):
@@ -81,6 +82,8 @@ class WaveSolver2D:
         self._engine_sponge = None if sp_c is None else sp_c.copy()
         if self.tile is not None:
             _lib.check(self._lib.w2d_engine_set_tile(h, int(self.tile[0]), int(self.tile[1])))
+        if self.l2_hints:
+            _lib.check(self._lib.w2d_engine_set_l2_hints(h, 1))
         return h
 
     def close(self):

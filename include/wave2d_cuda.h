@@ -93,6 +93,8 @@ int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel);
 
 /* Kernel tile shape (warps per CTA, rows per warp); 0,0 restores the default. */
 int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp);
+/* L2 residency hints in the step kernel (keep p_curr, v^2 dt^2, p_next; stream p_prev). */
+int w2d_engine_set_l2_hints(w2d_engine* e, int on);
 
 /* forward_propagate_acoustic, wave_solver.py:128-186.  rec_out: (nt, n_rec);
  * snaps_out: (ceil(nt/interval), nz, nx) or NULL.  Indices already in range. */
