@@ -239,6 +239,7 @@ def run_ours(args, dist):
     if args.tile:
         solver.tile = tuple(int(t) for t in args.tile.split(","))
     solver.l2_hints = bool(args.l2_hints)
+    solver.set_launch(args.launch, bool(args.pdl))
     eng = solver._eng()
     K, W = args.steps, args.warmup
     n_sh = K + W
@@ -341,6 +342,7 @@ def run_ours(args, dist):
                           "dx": sv.dx, "dt": sv.dt, "receivers": int(len(sv.rec_ix)),
                           "shots_per_step": 1, "snapshot_interval": interval,
                           "storage": used, "tile": list(solver.tile or (4, 4)),
+                          "launch": args.launch, "pdl": bool(args.pdl),
                           "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
                "shots_per_s": K * dist.world / dev_s,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -426,7 +428,9 @@ def run_batched(args, dist):
 def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
     """Poisson arrivals at `rate` jobs/s; grid sides log-uniform from 128 x 256 to
     1024 x 4096 (times side_scale), nt uniform in [1000, 8000] (times nt_scale), 1-32
-    shots per job sharing the job's smoothed faulted model; 80 % acoustic / 20 % elastic."""
+    shots per job sharing the job's smoothed faulted model; 80 % acoustic / 20 % elastic.
+    An elastic shot costs about ten acoustic ones (five fields, gradient with
+    recomputation), so elastic jobs get half the grid sides and 1-4 shots."""
     from das_gb300.batch import ShotJob
     from das_gb300.serving import poisson_trace
     from das_gb300.synthetic import _layered_faulted
@@ -436,9 +440,11 @@ def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
     def make(i, rng):
         nz = int(np.exp(rng.uniform(np.log(128), np.log(1024))) * side_scale)
         nx = int(np.exp(rng.uniform(np.log(256), np.log(4096))) * side_scale)
-        nz, nx = max(nz, 48), max(nx, 96)
         nt = max(64, int(rng.integers(1000, 8001) * nt_scale))
         kind = "elastic" if rng.uniform() < 0.2 else "acoustic"
+        if kind == "elastic":
+            nz, nx = nz // 2, nx // 2
+        nz, nx = max(nz, 48), max(nx, 96)
         d = 5.0
         zmax = (nz - 1) * d
         faults = [(rng.uniform(0.2, 0.8) * (nx - 1) * d, rng.uniform(45.0, 80.0),
@@ -447,7 +453,7 @@ def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
         v = gaussian_filter(v, 3.0).astype(np.float32)
         dt = 5e-4
         w, _ = ricker_wavelet(float(rng.uniform(3.0, 5.0)), dt, nt * dt)
-        n_sh = int(rng.integers(1, 33))
+        n_sh = int(rng.integers(1, 33)) if kind == "acoustic" else int(rng.integers(1, 5))
         if kind == "elastic":
             # shear velocity from the same model; vertical-strain observations
             vs = (v / 1.73).astype(np.float32)  # vp = 1.73 vs = v: same CFL as the acoustic
@@ -574,7 +580,8 @@ def run_served(args, dist):
                 "config": {"workload": f"Poisson trace of {len(trace)} jobs at {args.serve_rate} "
                                        f"jobs/s, sides log-uniform 128x256..1024x4096 x "
                                        f"{args.serve_side_scale}, nt U[1000,8000] x "
-                                       f"{args.serve_nt_scale}, 1-32 shots/job",
+                                       f"{args.serve_nt_scale}, 1-32 shots/job; elastic "
+                                       f"jobs half the sides, 1-4 shots",
                            "elastic_jobs_in_trace": n_el, "tile": list(tile),
                            "steps_per_launch": args.spl, "launches_per_graph": args.lpg},
                 "served": st, "plain_loop": plain,
@@ -591,6 +598,8 @@ def main():
                     choices=["large", "batched", "served", "elastic"])
     ap.add_argument("--el-nt", type=int, default=6000)
     ap.add_argument("--l2-hints", type=int, default=0)
+    ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
+    ap.add_argument("--pdl", type=int, default=1)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)

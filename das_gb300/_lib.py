@@ -49,6 +49,7 @@ _SIGS = {
     "w2d_engine_set_tile": (c_int, [c_void_p, c_int, c_int]),
     "w2d_engine_set_memory_budget": (c_int, [c_void_p, c_ull]),
     "w2d_engine_set_l2_hints": (c_int, [c_void_p, c_int]),
+    "w2d_engine_set_launch": (c_int, [c_void_p, c_int, c_int]),
     "w2d_forward": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
                             c_void_p, c_void_p, c_int]),
     "w2d_backward_correlate": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_int,
@@ -57,6 +58,7 @@ _SIGS = {
                                  c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "w2d_stack_reset": (c_int, [c_void_p]),
     "w2d_stack_read": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "w2d_post_stack": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "w2d_shot_stage": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int]),
     "w2d_migrate_staged": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int, c_int,
                                    c_int, c_void_p, c_void_p]),
@@ -83,6 +85,9 @@ _SIGS = {
     "w2d_batch_shot_bytes": (c_ull, [c_void_p]),
     "w2d_batch_free_bytes": (c_ull, [c_void_p]),
     "w2d_batch_submit": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
+    "w2d_batch_model_bytes": (c_ull, [c_void_p]),
+    "w2d_batch_submit_modelling": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
+    "w2d_batch_fetch_traces": (c_int, [c_void_p, c_int, c_void_p]),
     "w2d_batch_step": (c_int, [c_void_p, ctypes.POINTER(c_int)]),
     "w2d_batch_launch": (c_int, [c_void_p]),
     "w2d_batch_wait": (c_int, [c_void_p, ctypes.POINTER(c_int)]),

@@ -82,6 +82,52 @@ class ShotJob:
         return 2 * self.nx * self.nz * len(self.wavelet)
 
 
+@dataclass
+class ModelJob:
+    """One shot's forward modelling (WaveSolver2D.forward_propagate_acoustic with
+    snapshots off): its result is the (nt, n_receivers) gather of p_next samples."""
+    nx: int
+    nz: int
+    dx: float
+    dz: float
+    dt: float
+    vel: np.ndarray
+    wavelet: np.ndarray
+    receiver_ix: np.ndarray
+    source_ix: int
+    source_iz: int
+    receiver_iz: int = 2
+    n_sponge: int = 30
+    sponge_alpha: float = 0.0015
+    free_surface_top: bool = True
+    tag: object = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    def desc(self) -> _ShotDesc:
+        v = np.ascontiguousarray(self.vel, dtype=np.float32)
+        w = np.ascontiguousarray(self.wavelet, dtype=np.float32).reshape(-1)
+        if v.shape != (self.nz, self.nx):
+            raise ValueError("velocity model shape does not match (nz, nx)")
+        rix = normalize_indices(self.receiver_ix, self.nx, "receiver_ix")
+        self._keep = [v, w, rix]
+        return _ShotDesc(self.nx, self.nz, self.dx, self.dz, self.dt,
+                         1 if self.free_surface_top else 0, int(self.n_sponge),
+                         float(self.sponge_alpha), len(w), 1, len(rix),
+                         normalize_index(self.source_ix, self.nx, "source_ix"),
+                         normalize_index(self.source_iz, self.nz, "source_iz"),
+                         normalize_index(self.receiver_iz, self.nz, "receiver_iz"),
+                         v.ctypes.data, None, w.ctypes.data, None,
+                         rix.ctypes.data if len(rix) else None)
+
+    @property
+    def n_receivers(self) -> int:
+        return len(np.asarray(self.receiver_ix).reshape(-1))
+
+    @property
+    def counted_points(self) -> int:
+        return self.nx * self.nz * len(self.wavelet)
+
+
 class BatchEngine:
     """Persistent multi-shot RTM engine with admission by device-memory budget."""
 
@@ -116,16 +162,19 @@ class BatchEngine:
         return int(self._lib.w2d_batch_free_bytes(self._h))
 
     @staticmethod
-    def shot_bytes(job: ShotJob) -> int:
-        """Device bytes a shot occupies while admitted (upper bound)."""
+    def shot_bytes(job) -> int:
+        """Device bytes a job occupies while admitted (upper bound)."""
         d = job.desc()
-        return int(_lib.load().w2d_batch_shot_bytes(ctypes.byref(d)))
+        fn = "w2d_batch_model_bytes" if isinstance(job, ModelJob) else "w2d_batch_shot_bytes"
+        return int(getattr(_lib.load(), fn)(ctypes.byref(d)))
 
-    def submit(self, job: ShotJob) -> Optional[int]:
-        """Admit a shot; None when it does not fit in device memory right now."""
+    def submit(self, job) -> Optional[int]:
+        """Admit a ShotJob or ModelJob; None when it does not fit in device memory now."""
         d = job.desc()
         slot = ctypes.c_int(-1)
-        rc = self._lib.w2d_batch_submit(self._h, ctypes.byref(d), ctypes.byref(slot))
+        fn = (self._lib.w2d_batch_submit_modelling if isinstance(job, ModelJob)
+              else self._lib.w2d_batch_submit)
+        rc = fn(self._h, ctypes.byref(d), ctypes.byref(slot))
         if rc == 3:  # W2D_ENOMEM: wait for running shots to leave
             return None
         _lib.check(rc)
@@ -160,8 +209,21 @@ class BatchEngine:
         _lib.check(self._lib.w2d_batch_fetch(self._h, int(slot), img.ctypes.data, ill.ctypes.data))
         return img, ill
 
-    def run(self, jobs: Sequence[ShotJob]) -> Tuple[List[Tuple[np.ndarray, np.ndarray]], dict]:
-        """Migrate every job (continuous admission); results in job order and statistics."""
+    def fetch_traces(self, slot: int, nt: int, n_rec: int) -> np.ndarray:
+        tr = np.empty((nt, n_rec), np.float32)
+        _lib.check(self._lib.w2d_batch_fetch_traces(self._h, int(slot),
+                                                    tr.ctypes.data if tr.size else None))
+        return tr
+
+    def collect(self, slot: int, job):
+        """Result of a finished job: (image, illumination) or the modelled gather."""
+        if isinstance(job, ModelJob):
+            return self.fetch_traces(slot, len(job.wavelet), job.n_receivers)
+        return self.fetch(slot, job.nz, job.nx)
+
+    def run(self, jobs: Sequence) -> Tuple[list, dict]:
+        """Run every job (ShotJob or ModelJob, mixed freely; continuous admission);
+        results in job order and statistics."""
         results: List[Optional[Tuple[np.ndarray, np.ndarray]]] = [None] * len(jobs)
         pending = list(range(len(jobs)))
         running: Dict[int, int] = {}
@@ -192,6 +254,6 @@ class BatchEngine:
             launches += self.last_launches
             for slot in [s for s in running if self.finished(s)]:
                 j = running.pop(slot)
-                results[j] = self.fetch(slot, jobs[j].nz, jobs[j].nx)
+                results[j] = self.collect(slot, jobs[j])
         return results, {"device_ms": dev_ms, "counted_points": pts, "launches": launches,
                          "max_active": max_active}

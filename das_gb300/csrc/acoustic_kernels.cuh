@@ -388,8 +388,12 @@ __global__ void __launch_bounds__(WARPS * 32)
         prefetch_tensormap(&maps.curr);
         mbar_init(bar, 1);
         fence_mbar_init();
-        ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     }
+    // the set-up above overlaps the previous step's tail when launched as a
+    // programmatic dependent; nothing of the previous step is read before the wait
+    grid_dep_launch();
+    grid_dep_wait();
+    if (threadIdx.x == 0) ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     __syncthreads();
     if (!mbar_wait_bounded(bar, 0)) {
         if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
@@ -398,9 +402,101 @@ __global__ void __launch_bounds__(WARPS * 32)
     ac_tile_body<WARPS, RPW, SPONGE>(smem, g, s, x0, z0);
 }
 
+// Persistent form of the same tile-step: a grid sized to the resident capacity,
+// tiles handed out by an atomic counter, and the next tile's TMA boxes loading
+// into a second shared-memory stage while the current tile is computed.
+//
+// The counter is never reset between launches: every CTA takes tiles until it
+// draws an index past the last tile, so one launch draws exactly ntiles + gridDim.x
+// indices and the next launch starts at base + ntiles + gridDim.x.
+template <int WARPS, int RPW, int SPONGE>
+__global__ void __launch_bounds__(WARPS * 32)
+    acoustic_step_persistent(const __grid_constant__ AcMaps maps, const AcGeom g, const AcStep s,
+                             unsigned* counter, unsigned base, int tiles_x, int ntiles)
+{
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    extern __shared__ __align__(128) float smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::FLOATS);
+    __shared__ int s_tile[2];
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        prefetch_tensormap(&maps.curr);
+        prefetch_tensormap(&maps.prev);
+        prefetch_tensormap(&maps.vel);
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        fence_mbar_init();
+    }
+    grid_dep_launch();
+    grid_dep_wait();
+    auto issue = [&](int t, int stage) {
+        const int x0 = (t % tiles_x) * AC_TX, z0 = (t / tiles_x) * T::TZ;
+        ac_issue_loads<WARPS, RPW, SPONGE>(smem + stage * T::FLOATS, &maps, x0, z0, bar + stage,
+                                           g.l2_hints);
+    };
+    // an index outside [0, ntiles) ends the CTA's work
+    auto draw = [&]() {
+        const unsigned u = atomicAdd(counter, 1u) - base;
+        return u < (unsigned)ntiles ? (int)u : ntiles;
+    };
+    if (tid == 0) {
+        const int t = draw();
+        s_tile[0] = t;
+        if (t < ntiles) issue(t, 0);
+    }
+    __syncthreads();
+    for (int i = 0;; ++i) {
+        const int st = i & 1;
+        const int t = s_tile[st];
+        if (t >= ntiles) break;
+        bool next_issued = false;
+        if (tid == 0) {
+            // the other stage was released by the barrier that ended the previous tile
+            const int tn = draw();
+            s_tile[st ^ 1] = tn;
+            if (tn < ntiles) {
+                fence_proxy_async_shared();
+                issue(tn, st ^ 1);
+                next_issued = true;
+            }
+        }
+        const bool got = mbar_wait_bounded(bar + st, (unsigned)(i >> 1) & 1u);
+        if (__syncthreads_or(!got)) {
+            if (tid == 0) {
+                atomicOr(s.err, ERR_TMA_TIMEOUT);
+                // let the copy in flight into the other stage land before leaving
+                if (next_issued) mbar_wait_bounded(bar + (st ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            return;
+        }
+        const int x0 = (t % tiles_x) * AC_TX, z0 = (t / tiles_x) * T::TZ;
+        ac_tile_body<WARPS, RPW, SPONGE>(smem + st * T::FLOATS, g, s, x0, z0);
+        __syncthreads();
+    }
+}
+
+// Launch with optional programmatic stream serialization (the kernel may begin
+// while the previous kernel of the stream drains).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t st, int pdl, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int WARPS, int RPW, int SPONGE>
 inline cudaError_t launch_acoustic_step(const AcMaps& m, const AcGeom& g, const AcStep& s,
-                                        cudaStream_t st)
+                                        cudaStream_t st, int pdl = 0)
 {
     using T = AcTile<WARPS, RPW, SPONGE>;
     static bool attr_set = false;  // one attribute call per instantiation
@@ -412,8 +508,62 @@ inline cudaError_t launch_acoustic_step(const AcMaps& m, const AcGeom& g, const 
         attr_set = true;
     }
     dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
-    acoustic_step_kernel<WARPS, RPW, SPONGE><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
-    return cudaGetLastError();
+    if (!pdl) {
+        acoustic_step_kernel<WARPS, RPW, SPONGE><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
+        return cudaGetLastError();
+    }
+    return launch_ex(acoustic_step_kernel<WARPS, RPW, SPONGE>, grid, dim3(WARPS * 32),
+                     T::SMEM_BYTES, st, pdl, m, g, s);
+}
+
+// Shared memory of the persistent form: two stages and their barriers.
+template <int WARPS, int RPW, int SPONGE>
+constexpr size_t persistent_smem_bytes()
+{
+    return 2 * AcTile<WARPS, RPW, SPONGE>::FLOATS * 4u + 128;
+}
+
+// Resident CTAs of the persistent form on the current device (0 on error).
+template <int WARPS, int RPW, int SPONGE>
+inline int persistent_capacity()
+{
+    static int cap = -1;  // one query per instantiation
+    if (cap < 0) {
+        const int smem = (int)persistent_smem_bytes<WARPS, RPW, SPONGE>();
+        if (cudaFuncSetAttribute(acoustic_step_persistent<WARPS, RPW, SPONGE>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            return 0;
+        int per_sm = 0, dev = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, acoustic_step_persistent<WARPS, RPW, SPONGE>, WARPS * 32, smem) !=
+            cudaSuccess)
+            return 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cap = per_sm * sms;
+    }
+    return cap;
+}
+
+// One persistent launch; *base is advanced by the indices the launch draws.
+template <int WARPS, int RPW, int SPONGE>
+inline cudaError_t launch_acoustic_persistent(const AcMaps& m, const AcGeom& g, const AcStep& s,
+                                              cudaStream_t st, int pdl, unsigned* counter,
+                                              unsigned* base)
+{
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    const int cap = persistent_capacity<WARPS, RPW, SPONGE>();
+    if (cap <= 0) return cudaErrorInvalidConfiguration;
+    const int tiles_x = (g.nx + AC_TX - 1) / AC_TX;
+    const int ntiles = tiles_x * ((g.nz + T::TZ - 1) / T::TZ);
+    const int grid = cap < ntiles ? cap : ntiles;
+    const unsigned b = *base;
+    const cudaError_t e =
+        launch_ex(acoustic_step_persistent<WARPS, RPW, SPONGE>, dim3(grid), dim3(WARPS * 32),
+                  persistent_smem_bytes<WARPS, RPW, SPONGE>(), st, pdl, m, g, s, counter, b,
+                  tiles_x, ntiles);
+    if (e == cudaSuccess) *base = b + (unsigned)(ntiles + grid);
+    return e;
 }
 
 // Encode the TMA descriptors of one tile-step over pitched fields.

@@ -38,7 +38,10 @@ struct HostShot {
     float img_dt = 0.f;
     float* image = nullptr;
     float* illum = nullptr;
-    double counted_pts = 0;  // 2 * nx * nz * nt
+    double counted_pts = 0;  // grid points x phase steps
+    int mode = 0;            // 0: migration, 1: forward modelling
+    int nt = 0, n_rec = 0;
+    float* traces = nullptr;  // mode 1: (nt, n_rec)
 };
 
 }  // namespace
@@ -296,29 +299,40 @@ int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_p
 
 unsigned long long w2d_batch_free_bytes(w2d_batch* b) { return b ? largest_free(b) : 0ull; }
 
-unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d)
+}  // extern "C"
+
+namespace {
+
+// Arena bytes of one job: an upper bound that holds for every supported tile shape
+// (the smallest tile height is 16 rows).
+unsigned long long job_bytes(const w2d_shot_desc* d, int mode)
 {
-    if (!d || d->nx < 5 || d->nz < 5 || d->nt <= 0 || d->snapshot_interval <= 0) return 0;
+    if (!d || d->nx < 5 || d->nz < 5 || d->nt <= 0) return 0;
+    if (mode == 0 && d->snapshot_interval <= 0) return 0;
     const size_t ldx = (size_t)pitch_for(d->nx);
     const size_t plane = ldx * d->nz;
-    const size_t n_snaps = (size_t)(d->nt - 1) / d->snapshot_interval + 1;
-    const int tz = 32;  // upper bound on tiles: smallest supported tile height is 16
+    const size_t n_snaps = mode == 0 ? (size_t)(d->nt - 1) / d->snapshot_interval + 1 : 0;
+    const size_t planes = mode == 0 ? 10 + n_snaps : 4;  // waves, models, image, illum, snaps
     const size_t ntiles = (size_t)((d->nx + AC_TX - 1) / AC_TX) * ((d->nz + 15) / 16);
-    (void)tz;
-    size_t f = (10 + n_snaps) * plane + (size_t)d->nt + (size_t)d->nt * std::max(d->n_rec, 1) +
+    size_t f = planes * plane + (size_t)d->nt + (size_t)d->nt * std::max(d->n_rec, 1) +
                (size_t)std::max(d->n_sponge, 0) + 1 + (size_t)d->nx + 1 +
                (size_t)std::max(d->n_rec, 1) + ntiles + 64;
     return (unsigned long long)(f * 4 + 16 * kAlign);
 }
 
-int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
+// Admission of one job.  mode 0: migration (forward with snapshots and
+// illumination, then backward with imaging; 2 * nt phase steps).  mode 1: forward
+// modelling only, receivers sampled every step into an (nt, n_rec) gather.
+int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
 {
     W2D_CHECK_ARG(b && d && slot_out, "NULL argument");
     W2D_CHECK_ARG(d->nx >= 5 && d->nz >= 5, "grid must be at least 5 x 5");
     W2D_CHECK_ARG(d->dx > 0 && d->dz > 0 && d->dt > 0, "dx, dz, dt must be positive");
-    W2D_CHECK_ARG(d->nt > 0 && d->snapshot_interval > 0, "nt and interval must be positive");
-    W2D_CHECK_ARG(d->vel_fwd && d->vel_bwd && d->wavelet, "NULL model or wavelet");
-    W2D_CHECK_ARG(d->n_rec >= 0 && (d->n_rec == 0 || (d->data && d->rec_ix)), "bad receivers");
+    W2D_CHECK_ARG(d->nt > 0 && (mode == 1 || d->snapshot_interval > 0),
+                  "nt and interval must be positive");
+    W2D_CHECK_ARG(d->vel_fwd && (mode == 1 || d->vel_bwd) && d->wavelet, "NULL model or wavelet");
+    W2D_CHECK_ARG(d->n_rec >= 0 && (d->n_rec == 0 || ((mode == 1 || d->data) && d->rec_ix)),
+                  "bad receivers");
     W2D_CHECK_ARG(d->src_ix >= 0 && d->src_ix < d->nx && d->src_iz >= 0 && d->src_iz < d->nz,
                   "source index out of range");
     W2D_CHECK_ARG(d->rec_iz >= 0 && d->rec_iz < d->nz, "receiver_iz out of range");
@@ -336,20 +350,23 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     }
     const int nx = d->nx, nz = d->nz, ldx = pitch_for(nx), nt = d->nt, n_rec = d->n_rec;
     const size_t plane = (size_t)ldx * nz;
-    const int interval = d->snapshot_interval;
-    const size_t n_snaps = (size_t)(nt - 1) / interval + 1;
+    const int interval = mode == 0 ? d->snapshot_interval : 1;
+    const size_t n_snaps = mode == 0 ? (size_t)(nt - 1) / interval + 1 : 0;
+    const int n_waves = mode == 0 ? 6 : 3, n_models = mode == 0 ? 2 : 1;
+    const size_t n_img = mode == 0 ? 1 : 0;
     const int tz = b->warps * b->rpw;
     const int tiles_x = (nx + AC_TX - 1) / AC_TX, tiles_z = (nz + tz - 1) / tz;
     const int n_sp = std::max(d->n_sponge, 0);
-    // layout of the shot's block (each piece 256-byte aligned)
+    // layout of the shot's block (each piece 256-byte aligned); in mode 1 the
+    // data block holds the output gather
     size_t cur = 0;
     auto take = [&](size_t bytes) {
         const size_t o = cur;
         cur += (bytes + kAlign - 1) / kAlign * kAlign;
         return o;
     };
-    const size_t o_wave = take(6 * plane * 4), o_vel = take(2 * plane * 4),
-                 o_img = take(plane * 4), o_ill = take(plane * 4),
+    const size_t o_wave = take(n_waves * plane * 4), o_vel = take(n_models * plane * 4),
+                 o_img = take(n_img * plane * 4), o_ill = take(n_img * plane * 4),
                  o_snap = take(n_snaps * plane * 4), o_w = take((size_t)nt * 4),
                  o_data = take((size_t)nt * std::max(n_rec, 1) * 4), o_lut = take((n_sp + 1) * 4),
                  o_ptr = take((nx + 1) * 4), o_list = take(std::max(n_rec, 1) * 4),
@@ -389,19 +406,21 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     }
     std::vector<float> hlut(n_sp + 1, 1.0f);
     for (int k = 1; k <= n_sp; ++k) hlut[k] = cerjan_value(k, d->sponge_alpha);
-    // uploads: both models through the image plane as a pitched staging area
+    // uploads: the models pass through a pitched staging plane (the image plane,
+    // or in mode 1 the last wavefield plane), which is cleared again afterwards
+    float* stage = mode == 0 ? img : wave + 2 * plane;
     if (cudaMemsetAsync(base, 0, cur, st) != cudaSuccess) return undo(W2D_ECUDA);
-    for (int m = 0; m < 2; ++m) {
+    for (int m = 0; m < n_models; ++m) {
         const float* hv = m == 0 ? d->vel_fwd : d->vel_bwd;
-        if (cudaMemcpy2DAsync(img, (size_t)ldx * 4, hv, (size_t)nx * 4, (size_t)nx * 4, nz,
+        if (cudaMemcpy2DAsync(stage, (size_t)ldx * 4, hv, (size_t)nx * 4, (size_t)nx * 4, nz,
                               cudaMemcpyHostToDevice, st) != cudaSuccess)
             return undo(W2D_ECUDA);
-        v2dt2_kernel<<<grid_for(plane), 256, 0, st>>>(vel + m * plane, img, plane, dt2);
+        v2dt2_kernel<<<grid_for(plane), 256, 0, st>>>(vel + m * plane, stage, plane, dt2);
     }
-    if (cudaMemsetAsync(img, 0, plane * 4, st) != cudaSuccess ||
+    if (cudaMemsetAsync(stage, 0, plane * 4, st) != cudaSuccess ||
         cudaMemcpyAsync(wdev, d->wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice, st) ||
-        (n_rec > 0 && cudaMemcpyAsync(ddev, d->data, (size_t)nt * n_rec * 4,
-                                      cudaMemcpyHostToDevice, st)) ||
+        (mode == 0 && n_rec > 0 &&
+         cudaMemcpyAsync(ddev, d->data, (size_t)nt * n_rec * 4, cudaMemcpyHostToDevice, st)) ||
         cudaMemcpyAsync(lut, hlut.data(), hlut.size() * 4, cudaMemcpyHostToDevice, st) ||
         cudaMemcpyAsync(rptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, st) ||
         cudaMemcpyAsync(rlist, list.data(), list.size() * 4, cudaMemcpyHostToDevice, st))
@@ -431,25 +450,28 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     h.tiles_x = tiles_x;
     h.tiles_z = tiles_z;
     h.ntiles = tiles_x * tiles_z;
-    h.k_end = 2 * nt;
+    h.k_end = mode == 0 ? 2 * nt : nt;
     h.k0 = 0;
     h.maps_index = slot;
-    for (int i = 0; i < 6; ++i) h.wave[i] = wave + (size_t)i * plane;
-    h.snaps = snaps;
-    h.illum = ill;
-    h.image = img;
+    for (int i = 0; i < n_waves; ++i) h.wave[i] = wave + (size_t)i * plane;
+    h.snaps = mode == 0 ? snaps : nullptr;
+    h.illum = mode == 0 ? ill : nullptr;
+    h.image = mode == 0 ? img : nullptr;
     h.wavelet = wdev;
-    h.data = ddev;
+    h.data = mode == 0 ? ddev : nullptr;
     h.dt2_inj = (float)(d->dt * d->dt);
     h.img_dt = (float)(d->dt * (double)interval);
     h.done = done;
+    h.mode = mode;
+    h.traces = mode == 1 ? ddev : nullptr;
     BMaps maps;
-    for (int i = 0; i < 6; ++i) {
+    memset(&maps, 0, sizeof maps);
+    for (int i = 0; i < n_waves; ++i) {
         if ((rc = make_tensor_map_2d(&maps.curr[i], h.wave[i], nx, nz, ldx, AC_SW, tz + 4)) ||
             (rc = make_tensor_map_2d(&maps.prev[i], h.wave[i], nx, nz, ldx, AC_TX, tz)))
             return undo(rc);
     }
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < n_models; ++i)
         if ((rc = make_tensor_map_2d(&maps.vel[i], vel + i * plane, nx, nz, ldx, AC_TX, tz)))
             return undo(rc);
     if (cudaMemcpyAsync(b->d_shots + slot, &h, sizeof h, cudaMemcpyHostToDevice, st) ||
@@ -457,7 +479,7 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
         return undo(W2D_ECUDA);
     // first injections: w[0] into the forward p_curr, data row nt-1 into the backward p_curr
     inject_kernel<<<(nx + 255) / 256, 256, 0, st>>>(h.wave[1], h.g, wdev, nullptr, h.dt2_inj);
-    if (n_rec > 0)
+    if (mode == 0 && n_rec > 0)
         inject_kernel<<<(nx + 255) / 256, 256, 0, st>>>(h.wave[4], h.g, nullptr,
                                                         ddev + (size_t)(nt - 1) * n_rec, h.dt2_inj);
     if (!b->ready[slot] && cudaEventCreateWithFlags(&b->ready[slot], cudaEventDisableTiming)) {
@@ -479,14 +501,36 @@ int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
     hsh.nz = nz;
     hsh.ldx = ldx;
     hsh.plane = plane;
-    hsh.k_end = 2 * nt;
+    hsh.k_end = h.k_end;
     hsh.img_dt = h.img_dt;
-    hsh.image = img;
-    hsh.illum = ill;
-    hsh.counted_pts = 2.0 * nx * nz * nt;
+    hsh.image = h.image;
+    hsh.illum = h.illum;
+    hsh.counted_pts = (double)h.k_end * nx * nz;
+    hsh.mode = mode;
+    hsh.nt = nt;
+    hsh.n_rec = n_rec;
+    hsh.traces = h.traces;
     b->joining.push_back(slot);
     *slot_out = slot;
     return W2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d) { return job_bytes(d, 0); }
+
+unsigned long long w2d_batch_model_bytes(const w2d_shot_desc* d) { return job_bytes(d, 1); }
+
+int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
+{
+    return submit_job(b, d, 0, slot_out);
+}
+
+int w2d_batch_submit_modelling(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
+{
+    return submit_job(b, d, 1, slot_out);
 }
 
 int w2d_batch_launch(w2d_batch* b)
@@ -553,7 +597,8 @@ int w2d_batch_wait(w2d_batch* b, int* n_finished)
         b->last_pts += (double)(k1 - h.k0) * h.nx * h.nz;
         h.k0 += adv;
         if (h.k0 >= h.k_end) {
-            scale_kernel<<<grid_for(h.plane), 256, 0, b->st>>>(h.illum, h.plane, h.img_dt);
+            if (h.mode == 0)
+                scale_kernel<<<grid_for(h.plane), 256, 0, b->st>>>(h.illum, h.plane, h.img_dt);
             h.finished = true;
             ++fin;
         } else {
@@ -588,6 +633,7 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
     HostShot& h = b->hs[slot];
     W2D_CHECK_ARG(h.finished, "shot not finished");
+    W2D_CHECK_ARG(h.mode == 0, "a modelling job: fetch its gather with w2d_batch_fetch_traces");
     const size_t hp = (size_t)h.nx * 4, dp = (size_t)h.ldx * 4;
     if (image_out)
         W2D_CUDA_TRY(cudaMemcpy2DAsync(image_out, hp, h.image, dp, hp, h.nz,
@@ -595,6 +641,21 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
     if (illum_out)
         W2D_CUDA_TRY(cudaMemcpy2DAsync(illum_out, hp, h.illum, dp, hp, h.nz,
                                        cudaMemcpyDeviceToHost, b->st));
+    W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
+    arena_free(b, h.off, h.bytes);
+    h = HostShot();
+    return W2D_OK;
+}
+
+int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out)
+{
+    W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
+    HostShot& h = b->hs[slot];
+    W2D_CHECK_ARG(h.finished, "shot not finished");
+    W2D_CHECK_ARG(h.mode == 1, "a migration job: fetch its image with w2d_batch_fetch");
+    if (traces_out && h.n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(traces_out, h.traces, (size_t)h.nt * h.n_rec * 4,
+                                     cudaMemcpyDeviceToHost, b->st));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
     arena_free(b, h.off, h.bytes);
     h = HostShot();

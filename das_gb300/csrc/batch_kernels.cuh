@@ -42,6 +42,8 @@ struct BShot {
     const float* data;
     float dt2_inj, img_dt;
     unsigned* done;     // per tile: phase steps completed
+    int mode;           // 0: migration (forward + backward); 1: forward modelling only
+    float* traces;      // mode 1: (nt, n_rec) receiver samples
 };
 
 // TMA descriptors of one shot (global memory; CUtensorMap carries its own alignment).
@@ -153,7 +155,9 @@ __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1
             s.p_next = sh->wave[(it + 2) % 3];
             vi = 0;
             if (it + 1 < nt) s.inj_w = sh->wavelet + it + 1;
-            if (it % interval == 0) {
+            if (sh->mode == 1) {
+                s.rec_out = sh->traces + (size_t)it * sh->n_rec;
+            } else if (it % interval == 0) {
                 s.snap_out = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
                 s.illum = sh->illum;
             }

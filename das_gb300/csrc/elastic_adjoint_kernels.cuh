@@ -163,20 +163,28 @@ static __global__ void el_sample_kernel(ElGeom g, const float* vz, const int* re
 
 // Adjoint of the sampling: adj_vz += Dz-^T (residual) at each receiver, i.e. on
 // rows rec_iz (+c1), rec_iz-1 (-c1), rec_iz+1 (+c2), rec_iz-2 (-c2), cells of M only.
-static __global__ void el_adj_receivers(ElGeom g, float* adj_vz, const int* rec_ix, int n_rec,
-                                        int rec_iz, const float* resid)
+// One thread per column; receivers sharing a column (CSR rec_ptr / rec_list, in
+// index order) add into its cells one after another, so every cell receives its
+// contributions in receiver order.
+static __global__ void el_adj_receivers(ElGeom g, float* adj_vz, const int* rec_ptr,
+                                        const int* rec_list, int rec_iz, const float* resid)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;  // serial: receivers may share cells
-    const float k1 = 9.0f / 8.0f, k2 = -1.0f / 24.0f;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ix >= g.nx) return;
+    const int k0 = rec_ptr[ix], k1 = rec_ptr[ix + 1];
+    if (k0 == k1) return;
+    const float c1 = 9.0f / 8.0f, c2 = -1.0f / 24.0f;
     const int dz[4] = {0, -1, 1, -2};
-    const float cf[4] = {k1, -k1, k2, -k2};
-    for (int k = 0; k < n_rec; ++k) {
-        const float r = resid[k] * g.rdz;
-        for (int j = 0; j < 4; ++j) {
-            const int iz = rec_iz + dz[j], ix = rec_ix[k];
-            if (el_in_m(ix, iz, g.nx, g.nz, g.free_surface))
-                adj_vz[(size_t)iz * g.ldx + ix] += cf[j] * r;
-        }
+    const float cf[4] = {c1, -c1, c2, -c2};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int iz = rec_iz + dz[j];
+        if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) continue;
+        float* cell = adj_vz + (size_t)iz * g.ldx + ix;
+        float v = *cell;
+        for (int k = k0; k < k1; ++k)
+            v = fadd(v, fmul(cf[j], fmul(__ldg(resid + __ldg(rec_list + k)), g.rdz)));
+        *cell = v;
     }
 }
 

@@ -31,9 +31,12 @@ struct w2d_elastic {
     float* wavelet = nullptr;
     int w_cap = 0;
     int* rec = nullptr;
+    int* rec_ptr = nullptr;   // receivers by column (CSR, index order within a column)
+    int* rec_list = nullptr;
     int rec_cap = 0;
     float* traces = nullptr;
     size_t tr_cap = 0;
+    size_t rp_cap = 0, rl_cap = 0;
     int nt = 0, n_rec = 0, seg_len = 0, n_seg = 0, src_ix = 0, src_iz = 0, rec_iz = 0;
     bool have_forward = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -148,7 +151,7 @@ void w2d_elastic_destroy(w2d_elastic* e)
     if (e->st) cudaStreamSynchronize(e->st);
     for (void* p : {(void*)e->params, (void*)e->state, (void*)e->adj, (void*)e->tmp,
                     (void*)e->grad, (void*)e->ckpt, (void*)e->seg, (void*)e->wavelet,
-                    (void*)e->rec, (void*)e->traces})
+                    (void*)e->rec, (void*)e->rec_ptr, (void*)e->rec_list, (void*)e->traces})
         if (p) cudaFree(p);
     if (e->e0) cudaEventDestroy(e->e0);
     if (e->e1) cudaEventDestroy(e->e1);
@@ -181,6 +184,8 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
     size_t wc = e->w_cap, rcap = e->rec_cap;
     if ((rc = grow(&e->wavelet, (size_t)nt, &wc)) || (rc = grow(&e->rec, (size_t)n_rec, &rcap)) ||
         (rc = grow(&e->traces, (size_t)nt * n_rec, &e->tr_cap)) ||
+        (rc = grow(&e->rec_ptr, (size_t)e->nx + 1, &e->rp_cap)) ||
+        (rc = grow(&e->rec_list, (size_t)n_rec, &e->rl_cap)) ||
         (rc = grow(&e->ckpt, (size_t)e->n_seg * 5 * e->plane, &e->ckpt_planes)) ||
         (rc = grow(&e->seg, (size_t)(e->seg_len + 1) * 5 * e->plane, &e->seg_planes)))
         return rc;
@@ -193,6 +198,19 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
                                        e->st));
     W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice, e->st));
     W2D_CUDA_TRY(cudaMemcpyAsync(e->rec, rec_ix, (size_t)n_rec * 4, cudaMemcpyHostToDevice, e->st));
+    {
+        // receivers by column for the adjoint of the sampling
+        std::vector<int> ptr(e->nx + 1, 0), list(n_rec);
+        for (int k = 0; k < n_rec; ++k) ptr[rec_ix[k] + 1]++;
+        for (int i = 0; i < e->nx; ++i) ptr[i + 1] += ptr[i];
+        std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+        for (int k = 0; k < n_rec; ++k) list[fill[rec_ix[k]]++] = k;
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_ptr, ptr.data(), ptr.size() * 4,
+                                     cudaMemcpyHostToDevice, e->st));
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_list, list.data(), list.size() * 4,
+                                     cudaMemcpyHostToDevice, e->st));
+        W2D_CUDA_TRY(cudaStreamSynchronize(e->st));  // the host tables die here
+    }
     W2D_CUDA_TRY(cudaMemsetAsync(e->state, 0, 5 * e->plane * 4, e->st));
     W2D_CUDA_TRY(cudaEventRecord(e->e0, e->st));
     const ElGeom g = egeom(e);
@@ -237,8 +255,9 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
     float *glam = e->grad, *gmu = e->grad + P, *gbx = e->grad + 2 * P, *gbz = e->grad + 3 * P;
     dim3 blk(32, 8), grd((e->nx + 31) / 32, (e->nz + 7) / 8);
     // adjoint of u_nt: residual of the last trace row
-    el_adj_receivers<<<1, 32, 0, e->st>>>(g, a.vz, e->rec, n_rec, e->rec_iz,
-                                          e->traces + (size_t)(nt - 1) * n_rec);
+    const int rb = (e->nx + 127) / 128;
+    el_adj_receivers<<<rb, 128, 0, e->st>>>(g, a.vz, e->rec_ptr, e->rec_list, e->rec_iz,
+                                            e->traces + (size_t)(nt - 1) * n_rec);
     for (int sgi = e->n_seg - 1; sgi >= 0; --sgi) {
         const int a0 = sgi * e->seg_len, b0 = std::min(nt, a0 + e->seg_len);
         // recompute u_a0 .. u_b0 into the segment buffer
@@ -261,8 +280,9 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
             el_adj_k3<<<grd, blk, 0, e->st>>>(g, prm, a, r, f_curr, gbx, gbz);
             el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, a, r);
             if (n >= 1)
-                el_adj_receivers<<<1, 32, 0, e->st>>>(g, a.vz, e->rec, n_rec, e->rec_iz,
-                                                      e->traces + (size_t)(n - 1) * n_rec);
+                el_adj_receivers<<<rb, 128, 0, e->st>>>(g, a.vz, e->rec_ptr, e->rec_list,
+                                                        e->rec_iz,
+                                                        e->traces + (size_t)(n - 1) * n_rec);
         }
     }
     W2D_CUDA_TRY(cudaGetLastError());

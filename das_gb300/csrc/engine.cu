@@ -32,22 +32,39 @@ static bool tile_supported(int warps, int rpw)
            (warps == 4 && rpw == 4);
 }
 
-template <int W, int R>
-static cudaError_t launch_sp(int sponge_mode, const AcMaps& m, const AcGeom& g, const AcStep& s,
-                             cudaStream_t st)
+// How the step kernels are launched: one CTA per tile or persistent CTAs over a
+// tile counter, each optionally as a programmatic dependent of the previous step.
+struct LaunchMode {
+    int persistent = 0, pdl = 0;
+    unsigned* counter = nullptr;  // persistent: tile counter
+    unsigned* base = nullptr;     //   and the host copy of its launch base
+};
+
+template <int W, int R, int SP>
+static cudaError_t launch_one(const LaunchMode& lm, const AcMaps& m, const AcGeom& g,
+                              const AcStep& s, cudaStream_t st)
 {
-    if (sponge_mode == SPONGE_LUT) return launch_acoustic_step<W, R, SPONGE_LUT>(m, g, s, st);
-    if (sponge_mode == SPONGE_ARRAY) return launch_acoustic_step<W, R, SPONGE_ARRAY>(m, g, s, st);
-    return launch_acoustic_step<W, R, SPONGE_NONE>(m, g, s, st);
+    if (lm.persistent)
+        return launch_acoustic_persistent<W, R, SP>(m, g, s, st, lm.pdl, lm.counter, lm.base);
+    return launch_acoustic_step<W, R, SP>(m, g, s, st, lm.pdl);
 }
 
-static cudaError_t launch_step(TileShape t, int sponge_mode, const AcMaps& m, const AcGeom& g,
-                               const AcStep& s, cudaStream_t st)
+template <int W, int R>
+static cudaError_t launch_sp(int sponge_mode, const LaunchMode& lm, const AcMaps& m,
+                             const AcGeom& g, const AcStep& s, cudaStream_t st)
 {
-    if (t.warps == 4 && t.rpw == 8) return launch_sp<4, 8>(sponge_mode, m, g, s, st);
-    if (t.warps == 8 && t.rpw == 8) return launch_sp<8, 8>(sponge_mode, m, g, s, st);
-    if (t.warps == 4 && t.rpw == 4) return launch_sp<4, 4>(sponge_mode, m, g, s, st);
-    return launch_sp<8, 4>(sponge_mode, m, g, s, st);
+    if (sponge_mode == SPONGE_LUT) return launch_one<W, R, SPONGE_LUT>(lm, m, g, s, st);
+    if (sponge_mode == SPONGE_ARRAY) return launch_one<W, R, SPONGE_ARRAY>(lm, m, g, s, st);
+    return launch_one<W, R, SPONGE_NONE>(lm, m, g, s, st);
+}
+
+static cudaError_t launch_step(TileShape t, int sponge_mode, const LaunchMode& lm,
+                               const AcMaps& m, const AcGeom& g, const AcStep& s, cudaStream_t st)
+{
+    if (t.warps == 4 && t.rpw == 8) return launch_sp<4, 8>(sponge_mode, lm, m, g, s, st);
+    if (t.warps == 8 && t.rpw == 8) return launch_sp<8, 8>(sponge_mode, lm, m, g, s, st);
+    if (t.warps == 4 && t.rpw == 4) return launch_sp<4, 4>(sponge_mode, lm, m, g, s, st);
+    return launch_sp<8, 4>(sponge_mode, lm, m, g, s, st);
 }
 
 // ---- device buffer helper -------------------------------------------------------
@@ -93,6 +110,9 @@ struct w2d_engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     TileShape tile{4, 4};
     int l2_hints = 0;
+    int persistent = 0, pdl = 1;  // step launch mode (measured fastest: one CTA per tile + PDL)
+    DevBuf<unsigned> tile_counter;
+    unsigned counter_base = 0;
 
     int n_sponge = 0;
     DevBuf<float> sponge_lut, sponge_arr;
@@ -113,6 +133,7 @@ struct w2d_engine {
     DevBuf<float> snaps, ckpt;
     DevBuf<float> image, illum, stack_img, stack_ill;
     DevBuf<unsigned> err;
+    DevBuf<unsigned> scratch;  // small reductions (post-stack maximum)
     unsigned long long budget = 0;
     // inputs of the pass being run (engine buffers or a staged slot)
     const float* cur_w = nullptr;
@@ -184,7 +205,12 @@ int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcS
     m.prev = e->map_prev[prev];
     m.vel = e->map_vel[slot];
     m.sponge = e->map_sponge;
-    W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), m, g, s, e->stream));
+    LaunchMode lm;
+    lm.persistent = e->persistent;
+    lm.pdl = e->pdl;
+    lm.counter = e->tile_counter.p;
+    lm.base = &e->counter_base;
+    W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), lm, m, g, s, e->stream));
     e->last_launches++;
     return W2D_OK;
 }
@@ -350,6 +376,9 @@ int check_err(w2d_engine* e)
         snprintf(buf, sizeof buf, "device wait gave up (error bits 0x%x)", h);
         set_error(buf);
         W2D_CUDA_TRY(cudaMemsetAsync(e->err.p, 0, 4, e->stream));
+        // a CTA that stopped early drew fewer tile indices than the launch accounts for
+        W2D_CUDA_TRY(cudaMemsetAsync(e->tile_counter.p, 0, 4, e->stream));
+        e->counter_base = 0;
         return W2D_ETIMEOUT;
     }
     return W2D_OK;
@@ -407,9 +436,11 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
     }
     if ((rc = e->waves.ensure(6 * e->plane)) || (rc = e->v2dt2.ensure(2 * e->plane)) ||
         (rc = e->staging.ensure(e->plane)) || (rc = e->image.ensure(e->plane)) ||
-        (rc = e->illum.ensure(e->plane)) || (rc = e->err.ensure(1)))
+        (rc = e->illum.ensure(e->plane)) || (rc = e->err.ensure(1)) ||
+        (rc = e->tile_counter.ensure(1)))
         return fail(rc);
-    if (cudaMemset(e->err.p, 0, 4) != cudaSuccess || cudaMemset(e->waves.p, 0, 6 * e->plane * 4) ||
+    if (cudaMemset(e->err.p, 0, 4) != cudaSuccess || cudaMemset(e->tile_counter.p, 0, 4) ||
+        cudaMemset(e->waves.p, 0, 6 * e->plane * 4) ||
         cudaMemset(e->v2dt2.p, 0, 2 * e->plane * 4)) {
         set_error("memset failed");
         return fail(W2D_ECUDA);
@@ -489,6 +520,7 @@ void w2d_engine_destroy(w2d_engine* e)
     e->rec_ptr.release();
     e->rec_list.release();
     e->err.release();
+    e->scratch.release();
     for (auto& b : e->st_w) b.release();
     for (auto& b : e->st_d) b.release();
     if (e->t0) cudaEventDestroy(e->t0);
@@ -509,6 +541,15 @@ int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
     W2D_CHECK_ARG(tile_supported(warps, rows_per_warp), "unsupported tile shape");
     e->tile = TileShape{warps, rows_per_warp};
     return ensure_tensor_maps(e);
+}
+
+int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->persistent = persistent ? 1 : 0;
+    e->pdl = pdl ? 1 : 0;
+    return W2D_OK;
 }
 
 int w2d_engine_set_l2_hints(w2d_engine* e, int on)
@@ -901,6 +942,111 @@ int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out)
     int rc;
     if ((rc = download_field(e, image_out, e->stack_img.p)) ||
         (rc = download_field(e, illum_out, e->stack_ill.p)))
+        return rc;
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return W2D_OK;
+}
+
+}  // extern "C"
+
+// ---- post-stack on the device (rtm_engine.py:145-158) ---------------------------
+namespace {
+
+__device__ __forceinline__ float ps_sponge(const AcGeom& g, const float* arr, int ix, int iz)
+{
+    if (arr) return arr[(size_t)iz * g.ldx + ix];
+    if (g.sponge_lut) {
+        const int d = sponge_dist(ix, iz, g.nx, g.nz, g.n_sponge, g.free_surface);
+        return d > 0 ? g.sponge_lut[d] : 1.0f;
+    }
+    return 1.0f;
+}
+
+// muted copies of the stack and the largest illumination (as ordered bits: >= 0)
+__global__ void ps_mute_kernel(AcGeom g, const float* arr, int mute, const float* img,
+                               const float* ill, float* img_out, float* ill_out, unsigned* maxbits)
+{
+    const size_t n = (size_t)g.ldx * g.nz;
+    unsigned local = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / g.ldx), ix = (int)(i % g.ldx);
+        float a = img[i], b = ill[i];
+        if (ix >= g.nx || (mute && ps_sponge(g, arr, ix, iz) < 0.99f)) {
+            a = 0.0f;
+            b = 0.0f;
+        }
+        img_out[i] = a;
+        ill_out[i] = b;
+        local = max(local, __float_as_uint(b));
+    }
+    atomicMax(maxbits, local);
+}
+
+// normalized = stacked / (sqrt(illum) + eps), eps = float32(1e-4) * max or 1e-12
+__global__ void ps_normalize_kernel(AcGeom g, const float* img, const float* ill,
+                                    const unsigned* maxbits, float* out)
+{
+    const float mx = __uint_as_float(*maxbits);
+    const float eps = mx > 0.0f ? fmul(1e-4f, mx) : 1e-12f;
+    const size_t n = (size_t)g.ldx * g.nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        out[i] = __fdiv_rn(img[i], fadd(__fsqrt_rn(ill[i]), eps));
+}
+
+// 3x3 Laplacian, 'same' size, symmetric boundary (edge sample repeated), then mute
+__global__ void ps_laplacian_kernel(AcGeom g, const float* arr, int mute, const float* img,
+                                    float kx, float kz, float kc, float* out)
+{
+    const size_t n = (size_t)g.ldx * g.nz;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / g.ldx), ix = (int)(i % g.ldx);
+        if (ix >= g.nx) {
+            out[i] = 0.0f;
+            continue;
+        }
+        const int xm = ix > 0 ? ix - 1 : 0, xp = ix < g.nx - 1 ? ix + 1 : g.nx - 1;
+        const int zm = iz > 0 ? iz - 1 : 0, zp = iz < g.nz - 1 ? iz + 1 : g.nz - 1;
+        const float* r = img + (size_t)iz * g.ldx;
+        float v = kz * img[(size_t)zm * g.ldx + ix] + kx * r[xm] + kc * r[ix] + kx * r[xp] +
+                  kz * img[(size_t)zp * g.ldx + ix];
+        if (mute && ps_sponge(g, arr, ix, iz) < 0.99f) v = 0.0f;
+        out[i] = v;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int w2d_post_stack(w2d_engine* e, int mute_sponge, float* raw_out, float* laplacian_out,
+                   float* normalized_out)
+{
+    W2D_CHECK_ARG(e && raw_out && laplacian_out && normalized_out, "NULL argument");
+    W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
+    int rc;
+    if ((rc = e->snaps.ensure(2 * e->plane)) || (rc = e->scratch.ensure(1))) return rc;
+    unsigned* maxbits = e->scratch.p;
+    float* lap = e->snaps.p;
+    float* nrm = e->snaps.p + e->plane;
+    const AcGeom g = geom(e);
+    const float* arr = e->use_arr ? e->sponge_arr.p : nullptr;
+    W2D_CUDA_TRY(cudaMemsetAsync(maxbits, 0, 4, e->stream));
+    ps_mute_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(g, arr, mute_sponge, e->stack_img.p,
+                                                             e->stack_ill.p, e->image.p,
+                                                             e->illum.p, maxbits);
+    ps_normalize_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(g, e->image.p, e->illum.p,
+                                                                  maxbits, nrm);
+    const double ix2 = 1.0 / ((double)e->dx * e->dx), iz2 = 1.0 / ((double)e->dz * e->dz);
+    ps_laplacian_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(
+        g, arr, mute_sponge, e->image.p, (float)ix2, (float)iz2, (float)(-2.0 * ix2 - 2.0 * iz2),
+        lap);
+    W2D_CUDA_TRY(cudaGetLastError());
+    if ((rc = download_field(e, raw_out, e->image.p)) ||
+        (rc = download_field(e, laplacian_out, lap)) ||
+        (rc = download_field(e, normalized_out, nrm)))
         return rc;
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
     return W2D_OK;

@@ -171,6 +171,21 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map)
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// Programmatic dependent launch.  launch_dependents lets the next kernel of the
+// stream (launched with programmatic stream serialization) be scheduled once every
+// CTA of this grid has issued it; wait blocks until the previous kernel of the
+// stream has completed and its memory operations are visible.  Both are no-ops
+// for a kernel launched without the attribute.
+__device__ __forceinline__ void grid_dep_launch()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+__device__ __forceinline__ void grid_dep_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // IEEE single-precision arithmetic with no contraction into FMA: the engine
 // evaluates every stencil in the reference's operation order so that float32
 // results are bit-identical to the reference C engine built without FMA.

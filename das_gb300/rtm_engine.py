@@ -108,10 +108,13 @@ class TSWRTMEngine:
             _lib.check(s._lib.w2d_migrate_shot(
                 eng, w.ctypes.data, len(w), six, siz, data.ctypes.data, rix.ctypes.data,
                 data.shape[1], riz, int(snapshot_interval), _STORAGE[self.storage], None, None))
-        stacked = np.empty((s.nz, s.nx), np.float32)
-        illum = np.empty((s.nz, s.nx), np.float32)
-        _lib.check(s._lib.w2d_stack_read(eng, stacked.ctypes.data, illum.ctypes.data))
-        return post_stack(s, stacked, illum, mute_sponge)
+        # mute, normalisation and Laplacian run on the device stack
+        raw, lap, norm = (np.empty((s.nz, s.nx), np.float32) for _ in range(3))
+        _lib.check(s._lib.w2d_post_stack(eng, 1 if mute_sponge else 0, raw.ctypes.data,
+                                         lap.ctypes.data, norm.ctypes.data))
+        return RTMResult(raw_image=raw, laplacian_image=lap, normalized_image=norm,
+                         grid_x=np.arange(s.nx) * s.dx, grid_z=np.arange(s.nz) * s.dz,
+                         dx=s.dx, dz=s.dz)
 
 
 def post_stack(solver: WaveSolver2D, stacked: np.ndarray, illum: np.ndarray,

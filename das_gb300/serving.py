@@ -163,6 +163,10 @@ class RTMServer:
                  "device_busy_frac": busy_ms / 1e3 / makespan if makespan else 0.0,
                  "offered_jobs_per_s": (len(trace) - 1) / span_jobs if span_jobs > 0 else None,
                  "max_active_shots": max_active}
+        for kind in sorted({r.kind for r in out}):
+            lk = [r.latency for r in out if r.kind == kind]
+            stats[kind] = {"jobs": len(lk), "p50_latency_s": percentile(lk, 50),
+                           "p99_latency_s": percentile(lk, 99)}
         return out, stats
 
 

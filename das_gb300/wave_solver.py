@@ -64,6 +64,9 @@ class WaveSolver2D:
         self.storage = "auto"
         self.tile = None  # (warps, rows_per_warp) or None for the default
         self.l2_hints = False  # L2 residency hints in the step kernel
+        # step launch: one CTA per tile ("grid") or persistent CTAs ("persistent");
+        # each optionally a programmatic dependent of the previous step (pdl)
+        self.launch = ("grid", True)
 
     # -- engine handle -----------------------------------------------------------
     def _eng(self):
@@ -84,7 +87,22 @@ class WaveSolver2D:
             _lib.check(self._lib.w2d_engine_set_tile(h, int(self.tile[0]), int(self.tile[1])))
         if self.l2_hints:
             _lib.check(self._lib.w2d_engine_set_l2_hints(h, 1))
+        if self.launch != ("grid", True):
+            self._apply_launch(h)
         return h
+
+    def _apply_launch(self, h):
+        kind, pdl = self.launch
+        if kind not in ("grid", "persistent"):
+            raise ValueError("launch kind must be 'grid' or 'persistent'")
+        _lib.check(self._lib.w2d_engine_set_launch(h, 1 if kind == "persistent" else 0,
+                                                   1 if pdl else 0))
+
+    def set_launch(self, kind: str = "grid", pdl: bool = True) -> None:
+        """Choose how the step kernels launch (results are identical in every mode)."""
+        self.launch = (kind, bool(pdl))
+        if self._engine is not None:
+            self._apply_launch(self._engine)
 
     def close(self):
         if getattr(self, "_engine", None) is not None:

@@ -95,6 +95,12 @@ int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel);
 int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp);
 /* L2 residency hints in the step kernel (keep p_curr, v^2 dt^2, p_next; stream p_prev). */
 int w2d_engine_set_l2_hints(w2d_engine* e, int on);
+/* Step launch mode (results are bit-identical in every mode): persistent = 0 one
+ * CTA per tile, 1 CTAs resident for the whole step taking tiles from a counter
+ * with the next tile's boxes loading while the current one is computed; pdl = 1
+ * launches each step as a programmatic dependent of the previous one, so its
+ * set-up overlaps the previous step's tail.  Default: persistent 0, pdl 1. */
+int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl);
 
 /* forward_propagate_acoustic, wave_solver.py:128-186.  rec_out: (nt, n_rec);
  * snaps_out: (ceil(nt/interval), nz, nx) or NULL.  Indices already in range. */
@@ -123,6 +129,11 @@ int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, in
 /* Device stack of migrated shots (rtm_engine.py:142-143). */
 int w2d_stack_reset(w2d_engine* e);
 int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out);
+/* Post-stack of the device stack (rtm_engine.py:145-158) on the device: mute where the
+ * sponge is below 0.99, illumination normalisation with eps = 1e-4 * max, 3x3
+ * Laplacian with symmetric edges; the three (nz, nx) images are copied out. */
+int w2d_post_stack(w2d_engine* e, int mute_sponge, float* raw_out, float* laplacian_out,
+                   float* normalized_out);
 
 /* Device-resident shot inputs: stage a shot's wavelet (nt) and data (nt, n_rec)
  * into engine-owned device memory under an integer slot, then migrate it with
@@ -216,6 +227,14 @@ unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d);
 unsigned long long w2d_batch_free_bytes(w2d_batch* b);
 /* Admit a shot; W2D_ENOMEM when it does not fit now (retry after a fetch). */
 int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out);
+/* Forward-modelling job in the same batch (the many-shot form of
+ * wave_solver.py:128-186 forward_propagate_acoustic without snapshots): vel_fwd is the
+ * model, vel_bwd, data and snapshot_interval are ignored, and the receivers'
+ * p_next samples of every step form an (nt, n_rec) gather, read back with
+ * w2d_batch_fetch_traces.  Modelling and migration jobs share one replay. */
+unsigned long long w2d_batch_model_bytes(const w2d_shot_desc* d);
+int w2d_batch_submit_modelling(w2d_batch* b, const w2d_shot_desc* d, int* slot_out);
+int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out);
 /* Replay the captured time loop once over all active shots (launch + wait). */
 int w2d_batch_step(w2d_batch* b, int* n_finished);
 /* The two halves of w2d_batch_step: launch returns at once (shots submitted while

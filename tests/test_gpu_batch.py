@@ -84,3 +84,56 @@ def test_batch_golden_migrate_shot(golden):
     (img, ill), = BatchEngine(arena_bytes=1 << 28, max_shots=4).run([job])[0]
     np.testing.assert_array_equal(img, g["ms_image"])
     np.testing.assert_array_equal(ill, g["ms_illum"])
+
+
+def test_batch_modelling_golden_mixed_with_migration(golden):
+    """Forward-modelling jobs (observed gathers) and migration jobs share one
+    replay; each gather equals the reference's forward traces, including the
+    edge-cell source, edge and duplicated receivers, receivers in free-surface
+    row 1 and a grid without a free surface."""
+    from das_gb300.batch import BatchEngine, ModelJob
+    g = golden("loops")
+    nx, nz, dx, dt, n, a, fs = g["grid"]
+    nx, nz, n = int(nx), int(nz), int(n)
+    dx, dt, a = float(dx), float(dt), float(a)
+    w, rq, vt = g["wavelet"], g["q_rec_ix"], g["vtrue"]
+    models = [ModelJob(nx, nz, dx, dx, dt, vt, w, np.arange(nx), 20, 2, 2, n, a, True),
+              ModelJob(nx, nz, dx, dx, dt, vt, w[:120], rq, 0, 2, 2, n, a, True),
+              ModelJob(nx, nz, dx, dx, dt, vt, w[:120], rq, 31, 1, 1, n, a, True),
+              ModelJob(nx, nz, dx, dx, dt, vt, w, np.arange(nx), 33, 6, 4, n, a, False)]
+    expect = [g["fwd_rec"], g["q_fwd_rec"], g["q_row1_rec"], g["nofs_rec"]]
+    jobs = [models[0], _job(1, 90, 260, 150), models[1], models[2], _job(2, 40, 130, 97, 3),
+            models[3]]
+    eng = BatchEngine(arena_bytes=1 << 30, max_shots=16, steps_per_launch=11, launches_per_graph=3)
+    results, stats = eng.run(jobs)
+    assert stats["counted_points"] == sum(j.counted_points for j in jobs)
+    for k, e in zip((0, 2, 3, 5), expect):
+        r = results[k]
+        assert r.shape == e.shape
+        np.testing.assert_array_equal(r, e)
+    for k in (1, 4):
+        img, ill = results[k]
+        ref_img, ref_ill = _alone(jobs[k])
+        np.testing.assert_array_equal(img, ref_img)
+        np.testing.assert_array_equal(ill, ref_ill)
+
+
+def test_batch_modelling_matches_engine_forward():
+    """Random grids: the batched gather equals WaveSolver2D.forward_propagate_acoustic."""
+    from das_gb300.batch import BatchEngine, ModelJob
+    from das_gb300.wave_solver import WaveSolver2D
+    jobs = []
+    for k, (nz, nx, nt, ns, fs) in enumerate([(70, 300, 140, 20, True), (41, 97, 77, -1, True),
+                                               (128, 520, 90, 12, False)]):
+        base = _job(30 + k, nz, nx, nt, n_sponge=ns, fs=fs)
+        jobs.append(ModelJob(nx, nz, base.dx, base.dz, base.dt, base.vel_fwd, base.wavelet,
+                             base.receiver_ix, base.source_ix, base.source_iz, base.receiver_iz,
+                             ns, base.sponge_alpha, fs))
+    results, _ = BatchEngine(arena_bytes=1 << 29, max_shots=8, steps_per_launch=16,
+                             launches_per_graph=2).run(jobs)
+    for j, tr in zip(jobs, results):
+        s = WaveSolver2D(j.nx, j.nz, j.dx, j.dz, j.dt, j.n_sponge, j.sponge_alpha,
+                         j.free_surface_top)
+        ref, _ = s.forward_propagate_acoustic(j.vel, j.wavelet, j.source_ix, j.source_iz,
+                                              j.receiver_ix, j.receiver_iz, False)
+        np.testing.assert_array_equal(tr, ref)
