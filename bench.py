@@ -386,11 +386,12 @@ def run_batched(args, dist):
     pts = sum(j.counted_points for j in jobs)
     tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
     tune_table = None
+    form = args.batch_form
     if args.autotune:
         from das_gb300.autotune import tune_batch
-        (tile, args.spl, args.lpg), tune_table = tune_batch(jobs, use_cache=False)
+        (tile, args.spl, args.lpg, form), tune_table = tune_batch(jobs, use_cache=False)
     eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=len(jobs), tile=tile,
-                      steps_per_launch=args.spl, launches_per_graph=args.lpg)
+                      steps_per_launch=args.spl, launches_per_graph=args.lpg, form=form)
     eng.run(jobs[: min(4, len(jobs))])  # warm-up: graph capture, first-touch of the arena
     t0 = time.perf_counter()
     _, st = eng.run(jobs)
@@ -414,7 +415,7 @@ def run_batched(args, dist):
            "config": {"workload": f"{len(jobs)} uneven virtual-source gathers (nx 400-2000, nz "
                                   f"200-600, dx 5 m, nt scale {args.batch_nt_scale})",
                       "tile": list(tile), "steps_per_launch": args.spl,
-                      "launches_per_graph": args.lpg, "arena_gb": args.arena_gb},
+                      "launches_per_graph": args.lpg, "form": form, "arena_gb": args.arena_gb},
            "gpts_per_s_wall": pts / wall / 1e9,
            "gpts_per_s_device": st["counted_points"] / (st["device_ms"] / 1e3) / 1e9,
            "wall_s": wall, "max_active_shots": st["max_active"],
@@ -540,7 +541,8 @@ def run_served(args, dist):
     n_el = sum(r.kind == "elastic" for r in trace)
     tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
     eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=4096, tile=tile,
-                      steps_per_launch=args.spl, launches_per_graph=args.lpg)
+                      steps_per_launch=args.spl, launches_per_graph=args.lpg,
+                      form=args.batch_form)
     from das_gb300.elastic import ElasticExecutor
     eng.run([s for r in trace if r.kind == "acoustic" for s in r.shots][:1])  # graph capture
     ex = ElasticExecutor()
@@ -583,6 +585,7 @@ def run_served(args, dist):
                                        f"{args.serve_nt_scale}, 1-32 shots/job; elastic "
                                        f"jobs half the sides, 1-4 shots",
                            "elastic_jobs_in_trace": n_el, "tile": list(tile),
+                           "form": args.batch_form,
                            "steps_per_launch": args.spl, "launches_per_graph": args.lpg},
                 "served": st, "plain_loop": plain,
                 "served_first_jobs": {"p50_latency_s": percentile(served_first, 50),
@@ -612,6 +615,7 @@ def main():
     ap.add_argument("--spl", type=int, default=16)
     ap.add_argument("--lpg", type=int, default=16)
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--batch-form", default="grid", choices=["grid", "queue"])
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

@@ -82,6 +82,7 @@ _SIGS = {
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
+    "w2d_batch_set_form": (c_int, [c_void_p, c_int]),
     "w2d_batch_shot_bytes": (c_ull, [c_void_p]),
     "w2d_batch_free_bytes": (c_ull, [c_void_p]),
     "w2d_batch_submit": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
@@ -98,6 +99,20 @@ _SIGS = {
                                 ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_ll)]),
     "w2d_engine_last_stats": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_ll),
                                       ctypes.POINTER(c_ll), ctypes.POINTER(c_float)]),
+    # virtual-source gathers
+    "w2d_xcorr_rows": (c_int, [c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "w2d_xcorr_create": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_void_p, c_int,
+                                 c_void_p, c_int, c_int]),
+    "w2d_xcorr_destroy": (None, [c_void_p]),
+    "w2d_xcorr_shape": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "w2d_xcorr_add": (c_int, [c_void_p, c_void_p]),
+    "w2d_xcorr_add_device": (c_int, [c_void_p, c_void_p]),
+    "w2d_xcorr_read": (c_int, [c_void_p, c_void_p, c_int]),
+    "w2d_time_derivative": (c_int, [c_void_p, c_int, c_int, ctypes.c_double, c_int, c_void_p]),
+    "w2d_virtual_branch": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p,
+                                   ctypes.POINTER(c_int)]),
+    "w2d_resample_linear": (c_int, [c_void_p, c_int, c_int, ctypes.c_double, ctypes.c_double,
+                                    c_int, c_void_p]),
 }
 
 

@@ -1,8 +1,9 @@
 """Autotuner for the launch configuration of the RTM kernels.
 
-* ``tune_batch``: tile shape of the persistent kernel, phase steps per launch and
-  launches per captured graph, chosen by timing the batched engine on a sample of
-  the workload's own shots (truncated in time).
+* ``tune_batch``: form of the batched engine (one launch per phase step, or the
+  persistent queue kernel), tile shape, phase steps per launch and launches per
+  replay, chosen by timing the batched engine on a sample of the workload's own
+  shots (truncated in time).
 * ``tune_plain``: tile shape of the per-shot step kernel for one grid, chosen by
   timing a short forward run.
 
@@ -21,8 +22,11 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 
-BATCH_CANDIDATES = [((4, 4), 16, 16), ((4, 4), 32, 8), ((8, 4), 16, 16), ((4, 4), 8, 32),
-                    ((8, 4), 32, 8), ((4, 8), 16, 16)]
+# (form, tile, steps per launch, launches per replay); in the grid form the last two
+# only set how many phase steps a replay covers
+BATCH_CANDIDATES = [("grid", (4, 4), 16, 16), ("grid", (8, 4), 16, 16), ("grid", (4, 8), 16, 16),
+                    ("queue", (4, 4), 16, 16), ("queue", (4, 4), 32, 8), ("queue", (8, 4), 16, 16),
+                    ("queue", (4, 4), 8, 32), ("queue", (8, 4), 32, 8), ("queue", (4, 8), 16, 16)]
 PLAIN_TILES = [(4, 4), (8, 4), (4, 8), (8, 8)]
 
 
@@ -57,31 +61,32 @@ def _truncate(job, nt):
 
 def tune_batch(jobs: Sequence, candidates=None, sample_shots: int = 24, nt_sample: int = 256,
                arena_bytes: int = 0, use_cache: bool = True) -> Tuple[tuple, List[dict]]:
-    """Best (tile, steps_per_launch, launches_per_graph) for this set of shots."""
+    """Best (tile, steps_per_launch, launches_per_graph, form) for this set of shots."""
     from .batch import BatchEngine
     pts = np.mean([j.nx * j.nz for j in jobs])
-    key = f"batch:{int(np.log2(max(pts, 1)))}:{len(jobs) >= 64}"
+    key = f"batch2:{int(np.log2(max(pts, 1)))}:{len(jobs) >= 64}"
     cache = _load_cache() if use_cache else {}
     if key in cache:
         c = cache[key]["best"]
-        return (tuple(c[0]), c[1], c[2]), cache[key]["table"]
+        return (tuple(c[0]), c[1], c[2], c[3]), cache[key]["table"]
     rng = np.random.default_rng(0)
     idx = rng.choice(len(jobs), size=min(sample_shots, len(jobs)), replace=False)
     sample = [_truncate(jobs[i], nt_sample) for i in idx]
     table = []
-    for tile, spl, lpg in (candidates or BATCH_CANDIDATES):
+    for form, tile, spl, lpg in (candidates or BATCH_CANDIDATES):
         eng = BatchEngine(arena_bytes=arena_bytes, max_shots=len(sample) + 1, tile=tile,
-                          steps_per_launch=spl, launches_per_graph=lpg)
+                          steps_per_launch=spl, launches_per_graph=lpg, form=form)
         eng.run(sample[:2])  # graph capture and first touch
         _, st = eng.run(sample)
         eng.close()
         g = st["counted_points"] / max(st["device_ms"], 1e-6) / 1e6
-        table.append({"tile": list(tile), "steps_per_launch": spl, "launches_per_graph": lpg,
-                      "device_gpts_per_s": g})
+        table.append({"form": form, "tile": list(tile), "steps_per_launch": spl,
+                      "launches_per_graph": lpg, "device_gpts_per_s": g})
     best = max(table, key=lambda r: r["device_gpts_per_s"])
-    cfg = (tuple(best["tile"]), best["steps_per_launch"], best["launches_per_graph"])
+    cfg = (tuple(best["tile"]), best["steps_per_launch"], best["launches_per_graph"],
+           best["form"])
     if use_cache:
-        _store_cache(key, {"best": [list(cfg[0]), cfg[1], cfg[2]], "table": table})
+        _store_cache(key, {"best": [list(cfg[0]), cfg[1], cfg[2], cfg[3]], "table": table})
     return cfg, table
 
 

@@ -3,9 +3,10 @@
 The reference migrates shots one after another (tsw_rtm/rtm_engine.py:125-143).
 Here many shots -- each with its own grid size, length, models, wavelet and
 receivers -- are admitted into a device memory arena while memory allows and
-advanced together by one persistent kernel per launch over a (step, shot, tile)
-work queue; the time loop is a captured CUDA graph; finished shots leave and
-new ones enter between graph replays.  Each shot's result is bit-identical to
+advanced together: by default one kernel launch per phase step covers every
+active shot's tiles (form "grid"), or one persistent kernel per launch walks a
+(step, shot, tile) work queue (form "queue"); finished shots leave and new ones
+enter between two replays.  Each shot's result is bit-identical to
 migrating it alone with ``TSWRTMEngine.migrate_shot``: the arithmetic of every
 cell is the same fused step, independent of what else is in the batch.
 """
@@ -132,15 +133,24 @@ class BatchEngine:
     """Persistent multi-shot RTM engine with admission by device-memory budget."""
 
     def __init__(self, arena_bytes: int = 0, max_shots: int = 1024, tile=(8, 4),
-                 steps_per_launch: int = 16, launches_per_graph: int = 8):
+                 steps_per_launch: int = 16, launches_per_graph: int = 8, form: str = "grid"):
         self._lib = _lib.load()
         h = ctypes.c_void_p()
         _lib.check(self._lib.w2d_batch_create(ctypes.byref(h), int(arena_bytes), int(max_shots)))
         self._h = h
         self.config = None
         self.set_config(tile, steps_per_launch, launches_per_graph)
+        self.set_form(form)
         self.last_ms = 0.0
         self.last_points = 0.0
+
+    def set_form(self, form: str) -> None:
+        """'grid': one launch per phase step over every active shot (default);
+        'queue': persistent kernel over a (step, shot, tile) queue.  Same results."""
+        if form not in ("grid", "queue"):
+            raise ValueError("form must be 'grid' or 'queue'")
+        _lib.check(self._lib.w2d_batch_set_form(self._h, 1 if form == "grid" else 0))
+        self.form = form
 
     def set_config(self, tile, steps_per_launch, launches_per_graph):
         _lib.check(self._lib.w2d_batch_set_config(self._h, int(tile[0]), int(tile[1]),

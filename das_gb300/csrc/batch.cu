@@ -2,12 +2,14 @@
 //
 // Shots of different grid sizes and lengths are admitted into a device memory
 // arena (admission by memory budget: a shot is taken when its wavefields,
-// snapshot store, models and inputs fit), advanced together by the persistent
-// work-queue kernel of batch_kernels.cuh, and retired as soon as their backward
-// pass ends.  The time loop is a CUDA graph of `chunks` launches of S phase steps
-// each (plus the counter reset and the per-chunk advance), replayed until the
-// active shots finish; shots can join or leave between two replays without
-// recapturing the graph because the active list lives in device memory.
+// snapshot store, models and inputs fit), advanced together by the kernels of
+// batch_kernels.cuh, and retired as soon as their last phase step ends.  One
+// "replay" advances every active shot by S * chunks phase steps: in the grid form
+// (default) as S * chunks launches of one phase step each over all active shots'
+// tiles, chained as programmatic dependents, plus one progress advance; in the
+// queue form as a CUDA graph of `chunks` persistent launches of S phase steps each
+// (plus the counter reset and the per-chunk advance).  Shots join or leave between
+// two replays; the active list lives in device memory.
 #include <string.h>
 
 #include <algorithm>
@@ -66,6 +68,8 @@ struct w2d_batch {
     bool active_dirty = true;
     int warps = 8, rpw = 4, S = 16, chunks = 8;
     int grid = 0;
+    int form = 1;    // 1: one launch per phase step over all shots (grid form); 0: queue form
+    int t_all = 0;   // tiles of the active shots (grid form launch size)
     cudaGraphExec_t gexec = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<cudaEvent_t> ready;  // per slot: admission work finished
@@ -135,6 +139,32 @@ cudaError_t set_attr_and_occ(int* grid)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     *grid = std::max(1, per_sm) * sms;
     return cudaSuccess;
+}
+
+template <int W, int R>
+cudaError_t launch_batch_step(const BatchStepArgs& a, int grid, cudaStream_t st, int pdl)
+{
+    using T = AcTile<W, R, SPONGE_LUT>;
+    static bool attr_set = false;  // one attribute call per instantiation
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(acoustic_batch_step_kernel<W, R>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)T::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    return launch_ex(acoustic_batch_step_kernel<W, R>, dim3(grid), dim3(W * 32), T::SMEM_BYTES,
+                     st, pdl, a);
+}
+
+// pdl: launch as a programmatic dependent of the previous kernel; only when the
+// previous operation of the stream is that kernel.
+cudaError_t launch_step_cfg(w2d_batch* b, const BatchStepArgs& a, int pdl)
+{
+    if (b->warps == 4 && b->rpw == 4) return launch_batch_step<4, 4>(a, b->t_all, b->st, pdl);
+    if (b->warps == 4 && b->rpw == 8) return launch_batch_step<4, 8>(a, b->t_all, b->st, pdl);
+    if (b->warps == 8 && b->rpw == 8) return launch_batch_step<8, 8>(a, b->t_all, b->st, pdl);
+    return launch_batch_step<8, 4>(a, b->t_all, b->st, pdl);
 }
 
 template <int W, int R>
@@ -294,6 +324,15 @@ int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_p
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
+    return W2D_OK;
+}
+
+int w2d_batch_set_form(w2d_batch* b, int form)
+{
+    W2D_CHECK_ARG(b, "batch is NULL");
+    W2D_CHECK_ARG(form == 0 || form == 1, "form must be 0 (queue) or 1 (grid)");
+    W2D_CHECK_ARG(!b->in_flight, "change the form between replays only");
+    b->form = form;
     return W2D_OK;
 }
 
@@ -559,12 +598,39 @@ int w2d_batch_launch(w2d_batch* b)
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_prefix, prefix.data(), (n + 1) * 4,
                                      cudaMemcpyHostToDevice, b->st));
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_nact, &n, 4, cudaMemcpyHostToDevice, b->st));
+        b->t_all = prefix[n];
         b->active_dirty = false;
+    }
+    if (b->form == 1) {
+        // grid form: S * chunks launches, one phase step of every active shot each,
+        // then one advance of the shots' progress
+        const int steps = b->S * b->chunks;
+        BatchStepArgs a;
+        a.shots = b->d_shots;
+        a.maps = b->d_maps;
+        a.active = b->d_active;
+        a.tile_prefix = b->d_prefix;
+        a.n_active = (int)b->active.size();
+        a.max_shots = b->max_shots;
+        a.err = b->d_err;
+        W2D_CUDA_TRY(cudaEventRecord(b->e0, b->st));
+        for (int j = 0; j < steps; ++j) {
+            a.j = j;
+            W2D_CUDA_TRY(launch_step_cfg(b, a, j > 0 ? 1 : 0));
+        }
+        batch_advance_kernel<<<(b->max_shots + 127) / 128, 128, 0, b->st>>>(b->d_shots, b->d_active,
+                                                                             b->d_nact, steps);
+        W2D_CUDA_TRY(cudaGetLastError());
+        W2D_CUDA_TRY(cudaEventRecord(b->e1, b->st));
+        b->last_launches = steps + 1;
+        b->in_flight = true;
+        return W2D_OK;
     }
     if (!b->gexec && (rc = build_graph(b))) return rc;
     W2D_CUDA_TRY(cudaEventRecord(b->e0, b->st));
     W2D_CUDA_TRY(cudaGraphLaunch(b->gexec, b->st));
     W2D_CUDA_TRY(cudaEventRecord(b->e1, b->st));
+    b->last_launches = 2LL * b->chunks;
     b->in_flight = true;
     return W2D_OK;
 }
@@ -579,7 +645,6 @@ int w2d_batch_wait(w2d_batch* b, int* n_finished)
     W2D_CUDA_TRY(cudaMemcpyAsync(&herr, b->d_err, 4, cudaMemcpyDeviceToHost, b->st));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
     cudaEventElapsedTime(&b->last_ms, b->e0, b->e1);
-    b->last_launches = 2LL * b->chunks;
     if (herr) {
         char buf[96];
         snprintf(buf, sizeof buf, "persistent kernel stopped (error bits 0x%x)", herr);

@@ -1,5 +1,10 @@
-// batch_kernels.cuh -- persistent multi-shot RTM kernel over a (step, shot, tile)
-// work queue.
+// batch_kernels.cuh -- multi-shot RTM kernels: one launch per phase step over all
+// active shots (grid form), or a persistent kernel over a (step, shot, tile) work
+// queue (queue form).
+//
+// Grid form (acoustic_batch_step_kernel): every launch advances each active shot
+// by one phase step, one CTA per (shot, tile), launches chained as programmatic
+// dependents.  Queue form (acoustic_batch_kernel), described below.
 //
 // Many shots of different grid sizes and lengths advance together.  One launch
 // (a "chunk") covers S consecutive phase steps of every active shot; a shot's
@@ -76,6 +81,48 @@ __device__ __forceinline__ bool wait_counter(const unsigned* p, unsigned target,
     return false;
 }
 
+// The AcStep and TMA-descriptor indices of phase step k of one shot.
+__device__ __forceinline__ void batch_phase(const BShot* sh, int k, unsigned* err, AcStep& s,
+                                            int& ci, int& pi, int& vi)
+{
+    const int nt = sh->nt, interval = sh->interval;
+    s.snap_out = nullptr;
+    s.illum = nullptr;
+    s.rec_out = nullptr;
+    s.snap_in = nullptr;
+    s.image = nullptr;
+    s.img_dt = sh->img_dt;
+    s.inj_w = nullptr;
+    s.inj_data = nullptr;
+    s.dt2_inj = sh->dt2_inj;
+    s.err = err;
+    if (k < nt) {
+        const int it = k;
+        pi = it % 3;
+        ci = (it + 1) % 3;
+        s.p_next = sh->wave[(it + 2) % 3];
+        vi = 0;
+        if (it + 1 < nt) s.inj_w = sh->wavelet + it + 1;
+        if (sh->mode == 1) {
+            s.rec_out = sh->traces + (size_t)it * sh->n_rec;
+        } else if (it % interval == 0) {
+            s.snap_out = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
+            s.illum = sh->illum;
+        }
+    } else {
+        const int m = k - nt, it = nt - 1 - m;
+        pi = 3 + m % 3;
+        ci = 3 + (m + 1) % 3;
+        s.p_next = sh->wave[3 + (m + 2) % 3];
+        vi = 1;
+        if (it >= 1 && sh->n_rec > 0) s.inj_data = sh->data + (size_t)(it - 1) * sh->n_rec;
+        if (it % interval == 0) {
+            s.snap_in = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
+            s.image = sh->image;
+        }
+    }
+}
+
 // Registers capped so that four 256-thread (or eight 128-thread) CTAs fit per SM.
 template <int WARPS, int RPW>
 __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1)
@@ -134,45 +181,10 @@ __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1
         if (!s_ok) break;
 
         // the tile-step of phase step k
-        const int nt = sh->nt, interval = sh->interval;
         const BMaps* mp = a.maps + sh->maps_index;
         AcStep s;
-        s.snap_out = nullptr;
-        s.illum = nullptr;
-        s.rec_out = nullptr;
-        s.snap_in = nullptr;
-        s.image = nullptr;
-        s.img_dt = sh->img_dt;
-        s.inj_w = nullptr;
-        s.inj_data = nullptr;
-        s.dt2_inj = sh->dt2_inj;
-        s.err = a.err;
         int ci, pi, vi;
-        if (k < nt) {
-            const int it = k;
-            pi = it % 3;
-            ci = (it + 1) % 3;
-            s.p_next = sh->wave[(it + 2) % 3];
-            vi = 0;
-            if (it + 1 < nt) s.inj_w = sh->wavelet + it + 1;
-            if (sh->mode == 1) {
-                s.rec_out = sh->traces + (size_t)it * sh->n_rec;
-            } else if (it % interval == 0) {
-                s.snap_out = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
-                s.illum = sh->illum;
-            }
-        } else {
-            const int m = k - nt, it = nt - 1 - m;
-            pi = 3 + m % 3;
-            ci = 3 + (m + 1) % 3;
-            s.p_next = sh->wave[3 + (m + 2) % 3];
-            vi = 1;
-            if (it >= 1 && sh->n_rec > 0) s.inj_data = sh->data + (size_t)(it - 1) * sh->n_rec;
-            if (it % interval == 0) {
-                s.snap_in = sh->snaps + (size_t)(it / interval) * sh->g.ldx * sh->g.nz;
-                s.image = sh->image;
-            }
-        }
+        batch_phase(sh, k, a.err, s, ci, pi, vi);
         const int x0 = tx * AC_TX, z0 = tz * T::TZ;
         if (tid == 0) {
             fence_proxy_async_global();
@@ -196,6 +208,70 @@ __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1
             s_item = next;
         }
     }
+}
+
+struct BatchStepArgs {
+    BShot* shots;
+    const BMaps* maps;
+    const int* active;       // indices of active shots
+    const int* tile_prefix;  // prefix sums of their tile counts
+    int n_active;
+    int max_shots;           // size of the shot table (range check of active entries)
+    int j;                   // phase step k0 + j of every active shot
+    unsigned* err;
+};
+
+// Grid form: one launch advances every active shot by one phase step, one CTA
+// per (shot, tile); the launches after the first of a replay are programmatic
+// dependents of the one before, so a launch's set-up overlaps the previous one's
+// last wave (the first waits normally for the active-list copies and admission
+// events before it).  No waits between CTAs.
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32) acoustic_batch_step_kernel(const BatchStepArgs a)
+{
+    using T = AcTile<WARPS, RPW, SPONGE_LUT>;
+    extern __shared__ __align__(128) float smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    grid_dep_launch();
+    grid_dep_wait();  // shot progress and the active list come from earlier launches
+    const int r = blockIdx.x;
+    int lo = 0, hi = a.n_active - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(a.tile_prefix + mid) <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    const int slot = __ldg(a.active + lo);
+    const int t = r - __ldg(a.tile_prefix + lo);
+    if (slot < 0 || slot >= a.max_shots || t < 0) {  // inconsistent active list: skip, report
+        if (tid == 0) atomicOr(a.err, ERR_BAD_ITEM);
+        return;
+    }
+    const BShot* sh = a.shots + slot;
+    const int k = sh->k0 + a.j;
+    if (t >= sh->ntiles || k >= sh->k_end) return;
+    AcStep s;
+    int ci, pi, vi;
+    batch_phase(sh, k, a.err, s, ci, pi, vi);
+    const BMaps* mp = a.maps + sh->maps_index;
+    const int x0 = (t % sh->tiles_x) * AC_TX, z0 = (t / sh->tiles_x) * T::TZ;
+    if (tid == 0) {
+        mbar_expect_tx(bar, T::TX_BYTES);
+        tma_load_2d(smem, &mp->curr[ci], x0 - AC_HX, z0 - 2, bar);
+        tma_load_2d(smem + T::C_FLOATS, &mp->prev[pi], x0, z0, bar);
+        tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &mp->vel[vi], x0, z0, bar);
+    }
+    __syncthreads();
+    if (!mbar_wait_bounded(bar, 0)) {
+        if ((tid & 31) == 0) atomicOr(a.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    ac_tile_body<WARPS, RPW, SPONGE_LUT>(smem, sh->g, s, x0, z0);
 }
 
 // After each chunk: every active shot moves S phase steps on.

@@ -111,6 +111,7 @@ struct w2d_engine {
     TileShape tile{4, 4};
     int l2_hints = 0;
     int persistent = 0, pdl = 1;  // step launch mode (measured fastest: one CTA per tile + PDL)
+    bool chain = false;  // the last operation on the stream is a step kernel launched by step()
     DevBuf<unsigned> tile_counter;
     unsigned counter_base = 0;
 
@@ -207,10 +208,14 @@ int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcS
     m.sponge = e->map_sponge;
     LaunchMode lm;
     lm.persistent = e->persistent;
-    lm.pdl = e->pdl;
+    // a programmatic dependent only of a step kernel: after any other operation
+    // (copies, memsets, set-up kernels) the launch waits for the stream normally
+    lm.pdl = e->pdl && e->chain;
     lm.counter = e->tile_counter.p;
     lm.base = &e->counter_base;
+    e->chain = false;
     W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), lm, m, g, s, e->stream));
+    e->chain = true;
     e->last_launches++;
     return W2D_OK;
 }
@@ -286,11 +291,13 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
                       float dt2inj_f)
 {
     const AcGeom g = geom(e);
+    e->chain = false;  // the caller may have enqueued anything before these steps
     for (int it = it0; it < it1; ++it) {
         float* prev = e->wave(it % 3);
         float* curr = e->wave((it + 1) % 3);
         float* next = e->wave((it + 2) % 3);
         if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
+            e->chain = false;
             float* c = o.ckpt + (size_t)(it / o.ckpt_every) * 3 * e->plane;
             W2D_CUDA_TRY(cudaMemcpyAsync(c, prev, e->plane * 4, cudaMemcpyDeviceToDevice, e->stream));
             W2D_CUDA_TRY(cudaMemcpyAsync(c + e->plane, curr, e->plane * 4, cudaMemcpyDeviceToDevice,
@@ -334,6 +341,7 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
                        float img_dt, float dt2inj_f)
 {
     const AcGeom g = geom(e);
+    e->chain = false;  // the caller may have enqueued anything before these steps
     for (int it = it_hi; it >= it_lo; --it) {
         const int m = nt - 1 - it;
         float* next = e->wave(3 + (m + 2) % 3);
@@ -521,6 +529,7 @@ void w2d_engine_destroy(w2d_engine* e)
     e->rec_list.release();
     e->err.release();
     e->scratch.release();
+    e->tile_counter.release();
     for (auto& b : e->st_w) b.release();
     for (auto& b : e->st_d) b.release();
     if (e->t0) cudaEventDestroy(e->t0);

@@ -47,6 +47,7 @@ enum ErrBits : unsigned {
     ERR_TMA_TIMEOUT = 1u,
     ERR_DEP_TIMEOUT = 2u,  // a persistent CTA waited too long for a neighbour tile
     ERR_ABORT = 4u,        // set with any error: persistent CTAs stop taking work
+    ERR_BAD_ITEM = 8u,     // a batch CTA found an active-list entry out of range
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)

@@ -222,6 +222,10 @@ void w2d_batch_destroy(w2d_batch* b);
 /* Tile shape of the persistent kernel, phase steps per launch, launches per graph. */
 int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_per_launch,
                          int launches_per_graph);
+/* How a replay advances the shots: form 1 (default) one launch per phase step over
+ * every active shot's tiles; form 0 a persistent kernel over a (step, shot, tile)
+ * queue with per-tile dependency counters.  Results are identical. */
+int w2d_batch_set_form(w2d_batch* b, int form);
 /* Device bytes one shot needs (upper bound) and the largest free arena block. */
 unsigned long long w2d_batch_shot_bytes(const w2d_shot_desc* d);
 unsigned long long w2d_batch_free_bytes(w2d_batch* b);
@@ -259,6 +263,48 @@ int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes);
  * number of step kernels launched, recomputed forward steps, device ms. */
 int w2d_engine_last_stats(w2d_engine* e, int* storage_used, long long* step_launches,
                           long long* recomputed_steps, float* device_ms);
+
+/* ---- Part 4: virtual-source gathers (the step upstream of migration) ---------- */
+
+/* Rows the reference keeps of an FFT cross-correlation of nt-sample traces with
+ * n_lags = round(max_lag / dt) (interferometry.py:50-74): the Python slice
+ * [n_fft/2 - n_lags, n_fft/2 + n_lags + 1) of the fftshifted correlation,
+ * n_fft = 2^ceil(log2(2 nt - 1)); row i holds lag lag0 + i (in samples). */
+int w2d_xcorr_rows(int nt, int n_lags, int* lag0, int* n_rows);
+
+typedef struct w2d_xcorr w2d_xcorr;
+
+/* Cross-correlation stack of (nt, n_ch) data windows: for every source channel,
+ * c(l) = sum_t data[t, src] * data[t + l, rec] over the rows above and every
+ * receiver channel (compute_cross_correlation, interferometry.py:26-79, without
+ * the FFT: products and sums in float64, rounded to float32), added to a float32
+ * stack in window order (run_das_pipeline.py:202-213). */
+int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n_src,
+                     const int* rec_ch, int n_rec, int n_lags);
+void w2d_xcorr_destroy(w2d_xcorr* x);
+int w2d_xcorr_shape(w2d_xcorr* x, int* lag0, int* n_rows);
+/* Add one window: host (nt, n_ch) float32, or a device pointer. */
+int w2d_xcorr_add(w2d_xcorr* x, const float* data_host);
+int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev);
+/* Stack (n_src, n_rows, n_rec) to host memory; divide = 1 divides by
+ * float32(number of windows added) as run_das_pipeline.py:248-250 does. */
+int w2d_xcorr_read(w2d_xcorr* x, float* out_host, int divide);
+
+/* time_derivative_greens (interferometry.py:82-102) of an (n, nc) float32 array:
+ * scheme 0 = np.gradient(c, dt, axis=0) (bit-exact), 1 = i*omega*C(omega) at
+ * 2^ceil(log2(n)) points (float64 DFT). */
+int w2d_time_derivative(const float* in, int n, int nc, double dt, int scheme, float* out);
+
+/* Branch of build_virtual_shot_gather (interferometry.py:132-148): which = 0 causal
+ * (rows zero_idx..), 1 anticausal (rows zero_idx..0), 2 symmetric (float32 mean of
+ * the two over the shorter length).  *n_out = rows written. */
+int w2d_virtual_branch(const float* in, int n, int nc, int zero_idx, int which, float* out,
+                       int* n_out);
+
+/* resample_gather_to_sim_dt (run_das_pipeline.py:48-55): linear interpolation of each
+ * column from t = i*dt_orig to t = j*dt_sim, j < target_nt, zero outside the data. */
+int w2d_resample_linear(const float* in, int n, int nc, double dt_orig, double dt_sim,
+                        int target_nt, float* out);
 
 #ifdef __cplusplus
 }

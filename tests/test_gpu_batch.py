@@ -40,14 +40,15 @@ def _alone(job):
                                                job.snapshot_interval)
 
 
+@pytest.mark.parametrize("form", ["grid", "queue"])
 @pytest.mark.parametrize("tile,steps", [((8, 4), 16), ((4, 4), 7), ((4, 8), 33)])
-def test_batch_equals_single_shot(tile, steps):
+def test_batch_equals_single_shot(tile, steps, form):
     from das_gb300.batch import BatchEngine
     jobs = [_job(1, 90, 260, 150), _job(2, 40, 130, 97, interval=3),
             _job(3, 70, 400, 211, interval=1, fs=False), _job(4, 33, 77, 64, n_sponge=8),
             _job(5, 128, 300, 180, n_sponge=-1)]
     eng = BatchEngine(arena_bytes=1 << 30, max_shots=16, tile=tile, steps_per_launch=steps,
-                      launches_per_graph=3)
+                      launches_per_graph=3, form=form)
     results, stats = eng.run(jobs)
     assert stats["counted_points"] == sum(j.counted_points for j in jobs)
     for j, (img, ill) in zip(jobs, results):
@@ -104,8 +105,15 @@ def test_batch_modelling_golden_mixed_with_migration(golden):
     expect = [g["fwd_rec"], g["q_fwd_rec"], g["q_row1_rec"], g["nofs_rec"]]
     jobs = [models[0], _job(1, 90, 260, 150), models[1], models[2], _job(2, 40, 130, 97, 3),
             models[3]]
-    eng = BatchEngine(arena_bytes=1 << 30, max_shots=16, steps_per_launch=11, launches_per_graph=3)
-    results, stats = eng.run(jobs)
+    for form in ("grid", "queue"):
+        eng = BatchEngine(arena_bytes=1 << 30, max_shots=16, steps_per_launch=11,
+                          launches_per_graph=3, form=form)
+        results, stats = eng.run(jobs)
+        _check_modelling_mix(jobs, results, stats, expect)
+        eng.close()
+
+
+def _check_modelling_mix(jobs, results, stats, expect):
     assert stats["counted_points"] == sum(j.counted_points for j in jobs)
     for k, e in zip((0, 2, 3, 5), expect):
         r = results[k]
