@@ -105,8 +105,8 @@ _SIGS = {
                                  c_void_p, c_int, c_int]),
     "w2d_xcorr_destroy": (None, [c_void_p]),
     "w2d_xcorr_shape": (c_int, [c_void_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
-    "w2d_xcorr_add": (c_int, [c_void_p, c_void_p]),
-    "w2d_xcorr_add_device": (c_int, [c_void_p, c_void_p]),
+    "w2d_xcorr_add": (c_int, [c_void_p, c_void_p, c_int]),
+    "w2d_xcorr_add_device": (c_int, [c_void_p, c_void_p, c_int]),
     "w2d_xcorr_read": (c_int, [c_void_p, c_void_p, c_int]),
     "w2d_time_derivative": (c_int, [c_void_p, c_int, c_int, ctypes.c_double, c_int, c_void_p]),
     "w2d_virtual_branch": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p,

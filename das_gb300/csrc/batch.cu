@@ -448,7 +448,13 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
     // uploads: the models pass through a pitched staging plane (the image plane,
     // or in mode 1 the last wavefield plane), which is cleared again afterwards
     float* stage = mode == 0 ? img : wave + 2 * plane;
-    if (cudaMemsetAsync(base, 0, cur, st) != cudaSuccess) return undo(W2D_ECUDA);
+    // zero what is read before it is written: the wavefields, image and illumination
+    // (and the staging plane among them), the per-tile progress counters; the
+    // snapshot store, models, inputs and tables are written in full first
+    if (cudaMemsetAsync(base + o_wave, 0, o_vel - o_wave, st) != cudaSuccess ||
+        cudaMemsetAsync(base + o_img, 0, o_snap - o_img, st) != cudaSuccess ||
+        cudaMemsetAsync(base + o_done, 0, cur - o_done, st) != cudaSuccess)
+        return undo(W2D_ECUDA);
     for (int m = 0; m < n_models; ++m) {
         const float* hv = m == 0 ? d->vel_fwd : d->vel_bwd;
         if (cudaMemcpy2DAsync(stage, (size_t)ldx * 4, hv, (size_t)nx * 4, (size_t)nx * 4, nz,

@@ -9,10 +9,10 @@
 // Cross-correlation.  The reference evaluates c(l) = sum_t s[t] r[t + l] through a
 // zero-padded FFT at the data's precision (float32 under NumPy 2) and keeps rows
 // [n_fft/2 - n_lags, n_fft/2 + n_lags] of the fftshifted result with Python slice
-// semantics.  Here the same rows come from the direct sum: float32 samples,
-// products and accumulation in float64 (every product of two floats is exact in
-// float64), rounded once to float32.  The result is the correctly rounded
-// correlation up to the float64 summation error; the reference's float32 FFT
+// semantics.  Here the same rows come from the direct sum: float32 samples, every
+// product split exactly into two floats and accumulated in double-float
+// arithmetic (about 44 bits), rounded once to float32: the result is the
+// correlation rounded to float32 up to rare ties; the reference's float32 FFT
 // differs from it by a few 1e-8 in relative L2.  Each window's correlations are
 // added to a float32 stack in window order (the first window is copied), and the
 // stack is divided by float32(number of windows) on request, as the pipeline does.
@@ -76,11 +76,18 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
     const int rr = min(r, n_rec - 1);  // lanes past the last receiver compute a copy
     // row of Rp holding R[t + lag0 + row0] at t = 0
     const long long base = (long long)pad + lag0 + row0;
-    double acc[XC_LG];
+    // Double-float accumulation: each product is split exactly into p + e
+    // (p = fl(a*b), e = fma(a, b, -p)), p is added to hi with Knuth's two-sum
+    // (the rounding error goes to lo), and e joins lo.  The pair (hi, lo) carries
+    // about 44 significant bits, enough for the sum to round correctly to float32 in
+    // all but rare ties; it costs ten float32 operations per product, several times
+    // less than one float64 fused multiply-add on this GPU.
+    float hi[XC_LG], lo[XC_LG];
     float w[XC_LG];
 #pragma unroll
     for (int j = 0; j < XC_LG; ++j) {
-        acc[j] = 0.0;
+        hi[j] = 0.0f;
+        lo[j] = 0.0f;
         w[j] = Rp[(size_t)(base + j) * n_rec + rr];
     }
     for (int t0 = 0; t0 < nt; t0 += XC_CHUNK) {
@@ -90,9 +97,17 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
             s_src[i] = Ss[t0 + i];
         __syncthreads();
         for (int i = 0; i < len; ++i) {
-            const double sv = (double)s_src[i];
+            const float sv = s_src[i];
 #pragma unroll
-            for (int j = 0; j < XC_LG; ++j) acc[j] = fma(sv, (double)w[j], acc[j]);
+            for (int j = 0; j < XC_LG; ++j) {
+                const float p = __fmul_rn(sv, w[j]);
+                const float e = __fmaf_rn(sv, w[j], -p);
+                const float t = __fadd_rn(hi[j], p);
+                const float bp = __fsub_rn(t, hi[j]);
+                const float err = __fadd_rn(__fsub_rn(hi[j], __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                hi[j] = t;
+                lo[j] = __fadd_rn(lo[j], __fadd_rn(err, e));
+            }
 #pragma unroll
             for (int j = 0; j < XC_LG - 1; ++j) w[j] = w[j + 1];
             w[XC_LG - 1] = Rp[(size_t)(base + t0 + i + XC_LG) * n_rec + rr];
@@ -104,7 +119,7 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
         const int row = row0 + j;
         if (row >= n_rows) break;
         float* o = stack + ((size_t)s * n_rows + row) * n_rec + r;
-        const float c = __double2float_rn(acc[j]);
+        const float c = __fadd_rn(hi[j], lo[j]);
         *o = first ? c : __fadd_rn(*o, c);
     }
 }
@@ -276,9 +291,14 @@ int scratch_stream()
 
 struct w2d_xcorr {
     int nt = 0, n_ch = 0, n_src = 0, n_rec = 0, lag0 = 0, n_rows = 0, pad = 0, n_added = 0;
+    int n_lags = 0;
+    size_t r_rows = 0;  // rows of the zero-padded receiver buffer
+    int last_nt = 0;    // samples of the previous window (its rows must be cleared)
     int* d_src = nullptr;
     int* d_rec = nullptr;
-    float* d_data = nullptr;  // one (nt, n_ch) window
+    float* d_data[2] = {nullptr, nullptr};  // host windows land here, alternately
+    cudaEvent_t gathered[2] = {nullptr, nullptr};  // the gather that read d_data[i] is done
+    cudaStream_t st_copy = nullptr;
     float* d_s = nullptr;     // (n_src, nt)
     float* d_r = nullptr;     // (nt + 2*pad, n_rec), zero-padded
     float* d_stack = nullptr; // (n_src, n_rows, n_rec)
@@ -320,6 +340,7 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
     x->n_ch = n_ch;
     x->n_src = n_src;
     x->n_rec = n_rec;
+    x->n_lags = n_lags;
     w2d_xcorr_rows(nt, n_lags, &x->lag0, &x->n_rows);
     // rows of Rp read by the kernel: t + lag0 + row + j for t in [0, nt], row + j in
     // [0, rows rounded up to the CTA's lags + XC_LG]; padding keeps them inside
@@ -331,14 +352,18 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
         w2d_xcorr_destroy(x);
         return rc;
     };
-    if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess) {
-        set_error("stream creation failed");
+    if (cudaStreamCreateWithFlags(&x->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&x->st_copy, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->gathered[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&x->gathered[1], cudaEventDisableTiming) != cudaSuccess) {
+        set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
     }
-    size_t c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0;
+    size_t c0 = 0, c1 = 0, c2 = 0, c2b = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0;
     int rc;
     if ((rc = grow(&x->d_src, &c0, n_src)) || (rc = grow(&x->d_rec, &c1, n_rec)) ||
-        (rc = grow(&x->d_data, &c2, (size_t)nt * n_ch)) ||
+        (rc = grow(&x->d_data[0], &c2, (size_t)nt * n_ch)) ||
+        (rc = grow(&x->d_data[1], &c2b, (size_t)nt * n_ch)) ||
         (rc = grow(&x->d_s, &c3, (size_t)n_src * nt)) ||
         (rc = grow(&x->d_r, &c4, (size_t)r_rows * n_rec)) ||
         (rc = grow(&x->d_stack, &c5, (size_t)n_src * std::max(1, x->n_rows) * n_rec)) ||
@@ -352,6 +377,7 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
         set_error("cross-correlation set-up failed");
         return fail(W2D_ECUDA);
     }
+    x->r_rows = (size_t)r_rows;
     *out = x;
     return W2D_OK;
 }
@@ -360,9 +386,13 @@ void w2d_xcorr_destroy(w2d_xcorr* x)
 {
     if (!x) return;
     if (x->st) cudaStreamSynchronize(x->st);
-    for (void* p : {(void*)x->d_src, (void*)x->d_rec, (void*)x->d_data, (void*)x->d_s,
-                    (void*)x->d_r, (void*)x->d_stack, (void*)x->d_out})
+    if (x->st_copy) cudaStreamSynchronize(x->st_copy);
+    for (void* p : {(void*)x->d_src, (void*)x->d_rec, (void*)x->d_data[0], (void*)x->d_data[1],
+                    (void*)x->d_s, (void*)x->d_r, (void*)x->d_stack, (void*)x->d_out})
         if (p) cudaFree(p);
+    for (cudaEvent_t ev : x->gathered)
+        if (ev) cudaEventDestroy(ev);
+    if (x->st_copy) cudaStreamDestroy(x->st_copy);
     if (x->st) cudaStreamDestroy(x->st);
     delete x;
 }
@@ -375,31 +405,51 @@ int w2d_xcorr_shape(w2d_xcorr* x, int* lag0, int* n_rows)
     return W2D_OK;
 }
 
-int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev)
+int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt)
 {
     W2D_CHECK_ARG(x && data_dev, "NULL argument");
+    W2D_CHECK_ARG(nt >= 1 && nt <= x->nt, "window longer than the stack was created for");
+    int lag0 = 0, n_rows = 0;
+    w2d_xcorr_rows(nt, x->n_lags, &lag0, &n_rows);
+    // the reference's stack (ndarray +=) needs every window's correlation rows to agree
+    W2D_CHECK_ARG(lag0 == x->lag0 && n_rows == x->n_rows,
+                  "this window's correlation rows differ from the stack's");
     W2D_CHECK_ARG((x->n_rows + XC_LAGS - 1) / XC_LAGS <= 65535 && x->n_src <= 65535,
                   "too many lags or sources for one launch");
     if (x->n_rows > 0) {
-        xc_gather_kernel<<<grid_1d((size_t)x->nt * (x->n_rec + x->n_src)), 256, 0, x->st>>>(
-            data_dev, x->nt, x->n_ch, x->d_src, x->n_src, x->d_rec, x->n_rec, x->pad, x->d_s,
+        if (x->last_nt > nt)  // rows of a longer previous window must read as zero again
+            W2D_CUDA_TRY(cudaMemsetAsync(x->d_r + (size_t)(x->pad + nt) * x->n_rec, 0,
+                                         (size_t)(x->last_nt - nt) * x->n_rec * 4, x->st));
+        xc_gather_kernel<<<grid_1d((size_t)nt * (x->n_rec + x->n_src)), 256, 0, x->st>>>(
+            data_dev, nt, x->n_ch, x->d_src, x->n_src, x->d_rec, x->n_rec, x->pad, x->d_s,
             x->d_r);
         dim3 grid((x->n_rec + XC_RX - 1) / XC_RX, (x->n_rows + XC_LAGS - 1) / XC_LAGS, x->n_src);
-        xc_kernel<<<grid, dim3(XC_RX, XC_WY), 0, x->st>>>(x->d_s, x->d_r, x->nt, x->n_rec, x->pad,
+        xc_kernel<<<grid, dim3(XC_RX, XC_WY), 0, x->st>>>(x->d_s, x->d_r, nt, x->n_rec, x->pad,
                                                           x->lag0, x->n_rows, x->d_stack,
                                                           x->n_added == 0 ? 1 : 0);
         W2D_CUDA_TRY(cudaGetLastError());
     }
+    x->last_nt = nt;
     x->n_added++;
     return W2D_OK;
 }
 
-int w2d_xcorr_add(w2d_xcorr* x, const float* data_host)
+// The host window is copied on a second stream into one of two device buffers and
+// the call returns once that copy is done (the caller may reuse its array at
+// once); the correlation of the previous window keeps running meanwhile.
+int w2d_xcorr_add(w2d_xcorr* x, const float* data_host, int nt)
 {
     W2D_CHECK_ARG(x && data_host, "NULL argument");
-    W2D_CUDA_TRY(cudaMemcpyAsync(x->d_data, data_host, (size_t)x->nt * x->n_ch * 4,
-                                 cudaMemcpyHostToDevice, x->st));
-    return w2d_xcorr_add_device(x, x->d_data);
+    W2D_CHECK_ARG(nt >= 1 && nt <= x->nt, "window longer than the stack was created for");
+    const int b = x->n_added & 1;
+    W2D_CUDA_TRY(cudaStreamWaitEvent(x->st_copy, x->gathered[b], 0));
+    W2D_CUDA_TRY(cudaMemcpyAsync(x->d_data[b], data_host, (size_t)nt * x->n_ch * 4,
+                                 cudaMemcpyHostToDevice, x->st_copy));
+    W2D_CUDA_TRY(cudaStreamSynchronize(x->st_copy));
+    int rc = w2d_xcorr_add_device(x, x->d_data[b], nt);
+    if (rc) return rc;
+    W2D_CUDA_TRY(cudaEventRecord(x->gathered[b], x->st));
+    return W2D_OK;
 }
 
 int w2d_xcorr_read(w2d_xcorr* x, float* out_host, int divide)

@@ -3,7 +3,7 @@ resampling and a device-resident cross-correlation stack.
 
 * ``VirtualShotGather``              interferometry.py:13-23
 * ``compute_cross_correlation``      interferometry.py:26-79 (direct sum on the GPU,
-  float64 accumulation of float32 products, same rows and lag axis)
+  exact products accumulated in double-float arithmetic, same rows and lag axis)
 * ``time_derivative_greens``         interferometry.py:82-102
 * ``full_green_function``            interferometry.py:105-109
 * ``build_virtual_shot_gather``      interferometry.py:112-163
@@ -54,9 +54,10 @@ class CrossCorrelationStack:
     """Cross-correlations of several virtual-source channels against a set of receiver
     channels, stacked over data windows on the device.
 
-    ``add(window)`` takes one (nt, n_channels) float32 window (host array, or a CUDA
-    torch tensor through ``add_device``); ``result()`` returns {source channel: (ccfs,
-    lags)} exactly as the pipeline's stack after ``/= n_files``."""
+    ``add(window)`` takes one (nt_w, n_channels) float32 window with nt_w <= nt (host
+    array, or a CUDA torch tensor through ``add_device``) whose correlation rows agree
+    with the stack's (as NumPy's in-place sum requires); ``result()`` returns {source
+    channel: (ccfs, lags)} exactly as the pipeline's stack after ``/= n_files``."""
 
     def __init__(self, nt: int, n_channels: int, source_channels: Sequence[int],
                  receiver_indices: Optional[Sequence[int]], max_lag_seconds: float, dt: float):
@@ -80,19 +81,22 @@ class CrossCorrelationStack:
 
     def add(self, window: np.ndarray) -> None:
         w = np.ascontiguousarray(window, dtype=np.float32)
-        if w.shape != (self.nt, self.n_channels):
-            raise ValueError(f"window shape {w.shape} != {(self.nt, self.n_channels)}")
-        _lib.check(self._lib.w2d_xcorr_add(self._h, w.ctypes.data))
+        if w.ndim != 2 or w.shape[1] != self.n_channels or not 1 <= w.shape[0] <= self.nt:
+            raise ValueError(f"window shape {w.shape} does not fit (<= {self.nt}, "
+                             f"{self.n_channels})")
+        _lib.check(self._lib.w2d_xcorr_add(self._h, w.ctypes.data, w.shape[0]))
         self.windows += 1
 
     def add_device(self, window) -> None:
         """A CUDA tensor (nt, n_channels), float32, contiguous (synchronised first)."""
         import torch
-        if tuple(window.shape) != (self.nt, self.n_channels) or window.dtype != torch.float32 \
+        if window.dim() != 2 or window.shape[1] != self.n_channels or \
+                not 1 <= window.shape[0] <= self.nt or window.dtype != torch.float32 \
                 or not window.is_cuda or not window.is_contiguous():
-            raise ValueError("expected a contiguous float32 CUDA tensor (nt, n_channels)")
+            raise ValueError("expected a contiguous float32 CUDA tensor (nt_w, n_channels)")
         torch.cuda.current_stream().synchronize()
-        _lib.check(self._lib.w2d_xcorr_add_device(self._h, window.data_ptr()))
+        _lib.check(self._lib.w2d_xcorr_add_device(self._h, window.data_ptr(),
+                                                  int(window.shape[0])))
         self.windows += 1
 
     def result(self, divide: bool = True) -> Dict[int, Tuple[np.ndarray, np.ndarray]]:

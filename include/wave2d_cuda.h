@@ -16,6 +16,10 @@
  * das_gb300.rtm_engine) drives: one call runs an entire forward propagation,
  * backward propagation with imaging, or forward+backward migration of a shot,
  * with every time step, injection, sampling and imaging on the device.
+ *
+ * Part 3 is the batched engine (many shots advanced together, continuous
+ * admission), Part 4 the virtual-source gather generation upstream of migration
+ * (tsw_rtm/interferometry.py).
  */
 #ifndef WAVE2D_CUDA_H
 #define WAVE2D_CUDA_H
@@ -277,15 +281,16 @@ typedef struct w2d_xcorr w2d_xcorr;
 /* Cross-correlation stack of (nt, n_ch) data windows: for every source channel,
  * c(l) = sum_t data[t, src] * data[t + l, rec] over the rows above and every
  * receiver channel (compute_cross_correlation, interferometry.py:26-79, without
- * the FFT: products and sums in float64, rounded to float32), added to a float32
+ * the FFT: exact products summed in double-float, rounded to float32), added to a float32
  * stack in window order (run_das_pipeline.py:202-213). */
 int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n_src,
                      const int* rec_ch, int n_rec, int n_lags);
 void w2d_xcorr_destroy(w2d_xcorr* x);
 int w2d_xcorr_shape(w2d_xcorr* x, int* lag0, int* n_rows);
-/* Add one window: host (nt, n_ch) float32, or a device pointer. */
-int w2d_xcorr_add(w2d_xcorr* x, const float* data_host);
-int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev);
+/* Add one window of nt samples (nt no larger than the nt the stack was created for,
+ * and giving the same correlation rows): host (nt, n_ch) float32, or a device pointer. */
+int w2d_xcorr_add(w2d_xcorr* x, const float* data_host, int nt);
+int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt);
 /* Stack (n_src, n_rows, n_rec) to host memory; divide = 1 divides by
  * float32(number of windows added) as run_das_pipeline.py:248-250 does. */
 int w2d_xcorr_read(w2d_xcorr* x, float* out_host, int divide);
