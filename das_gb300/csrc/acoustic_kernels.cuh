@@ -395,8 +395,9 @@ __global__ void __launch_bounds__(WARPS * 32)
     grid_dep_wait();
     if (threadIdx.x == 0) ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     __syncthreads();
-    if (!mbar_wait_bounded(bar, 0)) {
-        if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        if (threadIdx.x == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
         return;
     }
     ac_tile_body<WARPS, RPW, SPONGE>(smem, g, s, x0, z0);

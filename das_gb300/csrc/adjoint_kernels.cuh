@@ -82,8 +82,9 @@ __global__ void __launch_bounds__(WARPS * 32)
         tma_load_2d(ta2, &maps.a2, x0, z0, bar);
     }
     __syncthreads();
-    if (!mbar_wait_bounded(bar, 0)) {
-        if ((threadIdx.x & 31) == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        if (threadIdx.x == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
         return;
     }
     for (int i = threadIdx.x; i < T::H_FLOATS; i += blockDim.x) tb[i] = tb[i] * ta1[i];

@@ -267,8 +267,9 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_step_kernel(const B
         tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &mp->vel[vi], x0, z0, bar);
     }
     __syncthreads();
-    if (!mbar_wait_bounded(bar, 0)) {
-        if ((tid & 31) == 0) atomicOr(a.err, ERR_TMA_TIMEOUT);
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        if (tid == 0) atomicOr(a.err, ERR_TMA_TIMEOUT);
         return;
     }
     ac_tile_body<WARPS, RPW, SPONGE_LUT>(smem, sh->g, s, x0, z0);

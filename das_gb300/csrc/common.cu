@@ -57,6 +57,33 @@ int make_tensor_map_2d(CUtensorMap* out, const float* base, int nx, int nz, int 
     return W2D_OK;
 }
 
+int make_tensor_map_3d(CUtensorMap* out, const float* base, int nx, int nz, int n_planes, int ldx,
+                       size_t plane_stride, int box_x, int box_z)
+{
+    CUtensorMap probe;
+    int rc = make_tensor_map_2d(&probe, base, nx, nz, ldx, box_x, box_z);  // loads the encoder
+    if (rc) return rc;
+    if ((plane_stride * sizeof(float)) % 16 || n_planes < 1) {
+        set_error("tensor map: plane stride not a multiple of 16 bytes");
+        return W2D_EINVAL;
+    }
+    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)nz, (cuuint64_t)n_planes};
+    cuuint64_t strides[2] = {(cuuint64_t)ldx * sizeof(float), (cuuint64_t)plane_stride * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_z, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = g_encode(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims,
+                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "cuTensorMapEncodeTiled (3D) failed (CUresult %d)", (int)r);
+        set_error(buf);
+        return W2D_ECUDA;
+    }
+    return W2D_OK;
+}
+
 // Frame distance of a cell, as float, exactly as the reference computes it
 // (tsw_rtm/c_engine/wave2d.c:246-256).
 static float frame_distance(int ix, int iz, int nx, int nz, int n, int fs)

@@ -39,11 +39,6 @@ struct ElParams {
     const float* sponge;  // pitched, or null
 };
 
-__device__ __forceinline__ bool el_in_m(int ix, int iz, int nx, int nz, int fs)
-{
-    return iz >= (fs ? 1 : 2) && iz < nz - 2 && ix >= 2 && ix < nx - 2;
-}
-
 // reads a[iz*L+ix] with zero outside the grid (rows/cols outside M hold zero)
 __device__ __forceinline__ float el_at(const float* a, int ix, int iz, int nx, int nz, int L)
 {
@@ -146,12 +141,8 @@ static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r)
     a.sxz[c] -= d_fwd_z(r.vx, ix, iz, nx, nz, L) * g.rdz + d_fwd_x(r.vz, ix, iz, nx, nz, L) * g.rdx;
 }
 
-// Forward pieces: source (vz += w * dt) and vertical-strain receivers of u_{n+1}.
-static __global__ void el_inject_kernel(float* vz, int ldx, int src_ix, int src_iz, const float* w,
-                                        float scale)
-{
-    if (threadIdx.x == 0 && blockIdx.x == 0) vz[(size_t)src_iz * ldx + src_ix] += w[0] * scale;
-}
+// Vertical-strain receivers of u_{n+1} (the source term is added by the step's
+// velocity phase, elastic_kernels.cuh).
 
 static __global__ void el_sample_kernel(ElGeom g, const float* vz, const int* rec_ix, int n_rec,
                                         int rec_iz, float* out)

@@ -39,6 +39,9 @@ struct w2d_elastic {
     size_t rp_cap = 0, rl_cap = 0;
     int nt = 0, n_rec = 0, seg_len = 0, n_seg = 0, src_ix = 0, src_iz = 0, rec_iz = 0;
     bool have_forward = false;
+    unsigned* err = nullptr;                // device error word of the step kernels
+    CUtensorMap map_state;                  // 3D map over the 5 planes of `state`
+    std::vector<CUtensorMap> seg_maps;      // one per state slot of `seg`
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     float last_ms = 0.f;
 
@@ -81,10 +84,41 @@ ElGeom egeom(w2d_elastic* e)
     return g;
 }
 
-ElFields efields(w2d_elastic* e, float* base)
+// Step n from the state at src to the state at dst (same pointer: in place), with
+// the source term w[n] * dt added to vz at the source cell first.
+int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, const float* src,
+             float* dst, int n)
 {
-    ElState s = e->S(base);
-    return ElFields{s.vx, s.vz, s.sxx, s.szz, s.sxz, e->P(0), e->P(1), e->P(2), e->P(3)};
+    ElMaps m;
+    m.src = msrc;
+    m.dst = mdst;
+    ElStep st;
+    st.src = src;
+    st.dst = dst;
+    st.plane = e->plane;
+    st.lam = e->P(0);
+    st.mu = e->P(1);
+    st.bx = e->P(2);
+    st.bz = e->P(3);
+    st.inj_ix = e->src_ix;
+    st.inj_iz = e->src_iz;
+    st.inj_w = e->wavelet + n;
+    st.err = e->err;
+    W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st));
+    return W2D_OK;
+}
+
+int check_el_err(w2d_elastic* e)
+{
+    unsigned h = 0;
+    W2D_CUDA_TRY(cudaMemcpyAsync(&h, e->err, 4, cudaMemcpyDeviceToHost, e->st));
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->st));
+    if (h) {
+        cudaMemsetAsync(e->err, 0, 4, e->st);
+        set_error("elastic step: a tile load did not complete");
+        return W2D_ETIMEOUT;
+    }
+    return W2D_OK;
 }
 
 bool on_m(const w2d_elastic* e, int iz, int ix)
@@ -92,14 +126,6 @@ bool on_m(const w2d_elastic* e, int iz, int ix)
     return iz >= (e->fs ? 1 : 2) && iz < e->nz - 2 && ix >= 2 && ix < e->nx - 2;
 }
 
-// one forward step n of the state at `base`: inject w[n], velocity + stress phase
-void fwd_step(w2d_elastic* e, float* base, int n)
-{
-    const ElState s = e->S(base);
-    el_inject_kernel<<<1, 32, 0, e->st>>>(s.vz, e->ldx, e->src_ix, e->src_iz, e->wavelet + n,
-                                          e->dt);
-    launch_elastic_step(egeom(e), efields(e, base), e->st);
-}
 
 }  // namespace
 
@@ -128,19 +154,22 @@ int w2d_elastic_create(w2d_elastic** out, int nx, int nz, float dx, float dz, do
         cudaEventCreate(&e->e0) || cudaEventCreate(&e->e1) ||
         cudaMalloc(&e->params, 5 * pb) || cudaMalloc(&e->state, 5 * pb) ||
         cudaMalloc(&e->adj, 5 * pb) || cudaMalloc(&e->tmp, 5 * pb) ||
-        cudaMalloc(&e->grad, 4 * pb)) {
+        cudaMalloc(&e->grad, 4 * pb) || cudaMalloc(&e->err, sizeof(unsigned))) {
         cudaGetLastError();
         set_error("elastic engine allocation failed");
         return fail(W2D_ENOMEM);
     }
     std::vector<float> sp((size_t)nx * nz);
     build_cerjan_sponge(sp.data(), nx, nz, n_sponge, sponge_alpha, e->fs);
-    if (cudaMemset(e->params, 0, 5 * pb) ||
+    if (cudaMemset(e->params, 0, 5 * pb) || cudaMemset(e->err, 0, sizeof(unsigned)) ||
         cudaMemcpy2D(e->P(4), (size_t)e->ldx * 4, sp.data(), (size_t)nx * 4, (size_t)nx * 4, nz,
                      cudaMemcpyHostToDevice)) {
         set_error("elastic engine set-up failed");
         return fail(W2D_ECUDA);
     }
+    int rc;
+    if ((rc = make_el_state_map(&e->map_state, e->state, nx, nz, e->ldx, e->plane)))
+        return fail(rc);
     *out = e;
     return W2D_OK;
 }
@@ -151,7 +180,8 @@ void w2d_elastic_destroy(w2d_elastic* e)
     if (e->st) cudaStreamSynchronize(e->st);
     for (void* p : {(void*)e->params, (void*)e->state, (void*)e->adj, (void*)e->tmp,
                     (void*)e->grad, (void*)e->ckpt, (void*)e->seg, (void*)e->wavelet,
-                    (void*)e->rec, (void*)e->rec_ptr, (void*)e->rec_list, (void*)e->traces})
+                    (void*)e->rec, (void*)e->rec_ptr, (void*)e->rec_list, (void*)e->traces,
+                    (void*)e->err})
         if (p) cudaFree(p);
     if (e->e0) cudaEventDestroy(e->e0);
     if (e->e1) cudaEventDestroy(e->e1);
@@ -191,6 +221,11 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
         return rc;
     e->w_cap = (int)wc;
     e->rec_cap = (int)rcap;
+    e->seg_maps.resize(e->seg_len + 1);
+    for (int i = 0; i <= e->seg_len; ++i)
+        if ((rc = make_el_state_map(&e->seg_maps[i], e->seg + (size_t)i * 5 * e->plane, e->nx,
+                                    e->nz, e->ldx, e->plane)))
+            return rc;
     const size_t hp = (size_t)e->nx * 4, dp = (size_t)e->ldx * 4;
     const float* src[4] = {lam, mu, bx, bz};
     for (int i = 0; i < 4; ++i)
@@ -219,7 +254,7 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
         if (n % e->seg_len == 0)
             W2D_CUDA_TRY(cudaMemcpyAsync(e->ckpt + (size_t)(n / e->seg_len) * 5 * e->plane, e->state,
                                          5 * e->plane * 4, cudaMemcpyDeviceToDevice, e->st));
-        fwd_step(e, e->state, n);
+        if ((rc = fwd_step(e, e->map_state, e->map_state, e->state, e->state, n))) return rc;
         el_sample_kernel<<<(n_rec + 127) / 128, 128, 0, e->st>>>(g, s.vz, e->rec, n_rec, rec_iz,
                                                                  e->traces + (size_t)n * n_rec);
     }
@@ -228,6 +263,7 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
     W2D_CUDA_TRY(cudaMemcpyAsync(traces_dev, e->traces, (size_t)nt * n_rec * 4,
                                  cudaMemcpyDeviceToDevice, e->st));
     W2D_CUDA_TRY(cudaStreamSynchronize(e->st));
+    if ((rc = check_el_err(e))) return rc;
     cudaEventElapsedTime(&e->last_ms, e->e0, e->e1);
     e->have_forward = true;
     return W2D_OK;
@@ -264,17 +300,17 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
         float* slot0 = e->seg;
         W2D_CUDA_TRY(cudaMemcpyAsync(slot0, e->ckpt + (size_t)sgi * 5 * P, 5 * pb,
                                      cudaMemcpyDeviceToDevice, e->st));
+        // out of place: slot n - a0 keeps u_n (without the w[n] source term)
         for (int n = a0; n < b0; ++n) {
-            float* nxt = e->seg + (size_t)(n + 1 - a0) * 5 * P;
-            W2D_CUDA_TRY(cudaMemcpyAsync(nxt, e->seg + (size_t)(n - a0) * 5 * P, 5 * pb,
-                                         cudaMemcpyDeviceToDevice, e->st));
-            fwd_step(e, nxt, n);
+            const int i = n - a0;
+            int rc;
+            if ((rc = fwd_step(e, e->seg_maps[i], e->seg_maps[i + 1], e->seg + (size_t)i * 5 * P,
+                               e->seg + (size_t)(i + 1) * 5 * P, n)))
+                return rc;
         }
         for (int n = b0 - 1; n >= a0; --n) {
             ElState f_next = e->S(e->seg + (size_t)(n + 1 - a0) * 5 * P);  // u_{n+1}
             ElState f_curr = e->S(e->seg + (size_t)(n - a0) * 5 * P);      // u_n
-            // the injection of w[n] into u_n's vz does not change its stresses, which
-            // are all K3 reads from u_n
             el_adj_k1<<<grd, blk, 0, e->st>>>(g, prm, a, t);
             el_adj_k2<<<grd, blk, 0, e->st>>>(g, prm, a, t, f_next, glam, gmu);
             el_adj_k3<<<grd, blk, 0, e->st>>>(g, prm, a, r, f_curr, gbx, gbz);
@@ -294,6 +330,8 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
             W2D_CUDA_TRY(cudaMemcpy2DAsync(outs[i], hp, e->grad + (size_t)i * P, dp, hp, e->nz,
                                            cudaMemcpyDeviceToDevice, e->st));
     W2D_CUDA_TRY(cudaStreamSynchronize(e->st));
+    int rc;
+    if ((rc = check_el_err(e))) return rc;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e->e0, e->e1);
     e->last_ms = ms;

@@ -3,13 +3,30 @@
 //
 // Follows tsw_rtm/c_engine/wave2d.c:95-212: a velocity phase that reads the
 // stresses, then a stress phase that reads the UPDATED velocities, each on rows
-// [1 if free surface else 2, nz-2) and columns [2, nx-2), each multiplied by the
-// sponge; then, with the free surface, szz = sxz = 0 on row 0 and sxx on row 0
-// from the free-surface relation.  The two phases are two launches (the stress
-// phase needs velocities of neighbouring tiles).  Where the reference reads row
-// -1 (sxz in the velocity phase, vz in the stress phase, at iz = 1) this engine
-// reads zero.  Arithmetic is float32 in the reference's operation order without
-// contraction into FMA.
+// [1 if free surface else 2, nz-2) and columns [2, nx-2) (the set M), each
+// multiplied by the sponge; then, with the free surface, szz = sxz = 0 on row 0
+// and sxx on row 0 from the free-surface relation.  The two phases are two
+// launches (the stress phase needs velocities of neighbouring tiles).  Where the
+// reference reads row -1 (sxz in the velocity phase, vz in the stress phase, at
+// iz = 1) this engine reads zero.  Arithmetic is float32 in the reference's
+// operation order without contraction into FMA.
+//
+// Data movement.  A state is five consecutive pitched planes (vx, vz, sxx, szz,
+// sxz) described by one 3D tensor map (x, row, plane).  Each CTA owns a 128 x TZ
+// tile; the fields a phase differentiates arrive as TMA boxes of 136 x (TZ+4)
+// (2-row and 4-column halo; the 4 keeps the box's x start 16-byte aligned; cells
+// outside the grid read as zero) on one mbarrier: sxx, sxz, szz for the velocity
+// phase, the new vx, vz for the stress phase.  Each lane owns four consecutive
+// x points (float4) and each warp walks RPW rows with a four-row register window
+// per field along z; x neighbours come from the adjacent lanes by warp shuffles
+// (shared memory only at the warp's two ends).  Fields used at one point only
+// (the velocities or stresses being updated, the parameters, the sponge) are
+// float4 loads from global memory.
+//
+// A step may run in place (src == dst) or out of place (dst receives every cell
+// of the tile: updated cells in M, copies of src elsewhere, and the free-surface
+// row).  The velocity phase can add a source term vz += w * dt at one cell of M
+// before the update (the modelling source of the elastic engine).
 #pragma once
 
 #include "w2d_common.cuh"
@@ -24,9 +41,32 @@ struct ElGeom {
     const float* sponge;  // pitched, or null
 };
 
-struct ElFields {
-    float *vx, *vz, *sxx, *szz, *sxz;
+// One launch of a phase: source and destination states (5 planes each, plane
+// stride `plane` floats), parameters (pitched planes), optional source term.
+struct ElStep {
+    const float* src;
+    float* dst;
+    size_t plane;
     const float *lam, *mu, *bx, *bz;
+    int inj_ix, inj_iz;       // velocity phase: vz[inj] += w[0] * dt first (inj_w non-null)
+    const float* inj_w;
+    unsigned* err;
+};
+
+struct ElMaps {
+    CUtensorMap src;  // 3D map over the source state's planes
+    CUtensorMap dst;  // 3D map over the destination state's planes
+};
+
+constexpr int EL_TX = 128;
+constexpr int EL_HX = 4;
+constexpr int EL_SW = EL_TX + 2 * EL_HX;
+enum { EL_VX = 0, EL_VZ = 1, EL_SXX = 2, EL_SZZ = 3, EL_SXZ = 4 };
+
+template <int WARPS, int RPW>
+struct ElTile {
+    static constexpr int TZ = WARPS * RPW;
+    static constexpr int BOX = (TZ + 4) * EL_SW;  // floats per box
 };
 
 // c1*(a[+s]-a[0]) + c2*(a[+2s]-a[-s])
@@ -42,90 +82,324 @@ __device__ __forceinline__ float el_dbwd(float am2, float am1, float a0, float a
     return fadd(fmul(k1, fsub(a0, am1)), fmul(k2, fsub(ap1, am2)));
 }
 
-static __global__ void __launch_bounds__(256) elastic_velocity_kernel(ElGeom g, ElFields f)
+__device__ __forceinline__ float el_c(const float4& v, int j)
 {
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iz = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z0 = g.free_surface ? 1 : 2;
-    if (ix < 2 || ix >= g.nx - 2 || iz < z0 || iz >= g.nz - 2) return;
-    const int L = g.ldx;
-    const size_t c = (size_t)iz * L + ix;
-    const float* sxx = f.sxx;
-    const float* sxz = f.sxz;
-    const float* szz = f.szz;
-    const float sxz_m2z = iz >= 2 ? __ldg(sxz + c - 2 * L) : 0.0f;
-    const float a = fmul(el_dfwd(__ldg(sxx + c - 1), __ldg(sxx + c), __ldg(sxx + c + 1),
-                                 __ldg(sxx + c + 2)),
-                         g.rdx);
-    const float b = fmul(el_dbwd(sxz_m2z, __ldg(sxz + c - L), __ldg(sxz + c), __ldg(sxz + c + L)),
-                         g.rdz);
-    float vx = fadd(f.vx[c], fmul(fmul(g.dt, __ldg(f.bx + c)), fadd(a, b)));
-    const float e = fmul(el_dbwd(__ldg(sxz + c - 2), __ldg(sxz + c - 1), __ldg(sxz + c),
-                                 __ldg(sxz + c + 1)),
-                         g.rdx);
-    const float h = fmul(el_dfwd(__ldg(szz + c - L), __ldg(szz + c), __ldg(szz + c + L),
-                                 __ldg(szz + c + 2 * L)),
-                         g.rdz);
-    float vz = fadd(f.vz[c], fmul(fmul(g.dt, __ldg(f.bz + c)), fadd(e, h)));
-    if (g.sponge) {
-        const float s = __ldg(g.sponge + c);
-        vx = fmul(vx, s);
-        vz = fmul(vz, s);
-    }
-    f.vx[c] = vx;
-    f.vz[c] = vz;
+    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
 }
 
-static __global__ void __launch_bounds__(256) elastic_stress_kernel(ElGeom g, ElFields f)
+// Row `srow` of a box as this lane's float4 plus the x neighbours it needs:
+// e[0..1] = x-2, x-1 of the first point; e[2..5] the four points; e[6..7] = x+4, x+5.
+__device__ __forceinline__ void el_xrow(const float* box, int srow, int lane, float e[8])
 {
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iz = blockIdx.y * blockDim.y + threadIdx.y;
-    const int L = g.ldx;
-    const float* vx = f.vx;
-    const float* vz = f.vz;
-    if (g.free_surface && iz == 0 && ix < g.nx) {
-        // free-surface row (wave2d.c:198-211)
-        f.szz[ix] = 0.0f;
-        f.sxz[ix] = 0.0f;
-        if (ix >= 2 && ix < g.nx - 2) {
-            const float l = __ldg(f.lam + ix), m = __ldg(f.mu + ix);
-            const float ex = fmul(el_dbwd(vx[ix - 2], vx[ix - 1], vx[ix], vx[ix + 1]), g.rdx);
-            const float num = fmul(fmul(4.0f, m), fadd(l, m));
-            const float den = fadd(fadd(l, fmul(2.0f, m)), 1e-8f);
-            f.sxx[ix] = fmul(__fdiv_rn(num, den), ex);
-        }
+    const float4 w = *reinterpret_cast<const float4*>(&box[srow * EL_SW + EL_HX + 4 * lane]);
+    float l2 = __shfl_up_sync(0xffffffffu, w.z, 1);
+    float l1 = __shfl_up_sync(0xffffffffu, w.w, 1);
+    float r1 = __shfl_down_sync(0xffffffffu, w.x, 1);
+    float r2 = __shfl_down_sync(0xffffffffu, w.y, 1);
+    if (lane == 0) {
+        l2 = box[srow * EL_SW + EL_HX - 2];
+        l1 = box[srow * EL_SW + EL_HX - 1];
+    }
+    if (lane == 31) {
+        r1 = box[srow * EL_SW + EL_HX + EL_TX];
+        r2 = box[srow * EL_SW + EL_HX + EL_TX + 1];
+    }
+    e[0] = l2;
+    e[1] = l1;
+    e[2] = w.x;
+    e[3] = w.y;
+    e[4] = w.z;
+    e[5] = w.w;
+    e[6] = r1;
+    e[7] = r2;
+}
+
+__device__ __forceinline__ float4 el_row4(const float* box, int srow, int lane)
+{
+    return *reinterpret_cast<const float4*>(&box[srow * EL_SW + EL_HX + 4 * lane]);
+}
+
+__device__ __forceinline__ bool el_in_m(int ix, int iz, int nx, int nz, int fs)
+{
+    return iz >= (fs ? 1 : 2) && iz < nz - 2 && ix >= 2 && ix < nx - 2;
+}
+
+// Store four values of one row: float4 when all four go out, else per point.
+__device__ __forceinline__ void el_store_row(float* dst, const float* src, size_t off, int ixb,
+                                             int iz, const ElGeom& g, const float u[4],
+                                             bool in_place)
+{
+    bool all = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) all &= el_in_m(ixb + j, iz, g.nx, g.nz, g.free_surface);
+    if (all) {
+        *reinterpret_cast<float4*>(dst + off) = make_float4(u[0], u[1], u[2], u[3]);
         return;
     }
-    const int z0 = g.free_surface ? 1 : 2;
-    if (ix < 2 || ix >= g.nx - 2 || iz < z0 || iz >= g.nz - 2) return;
-    const size_t c = (size_t)iz * L + ix;
-    const float vz_m2z = iz >= 2 ? vz[c - 2 * L] : 0.0f;
-    const float ex = fmul(el_dbwd(vx[c - 2], vx[c - 1], vx[c], vx[c + 1]), g.rdx);
-    const float ez = fmul(el_dbwd(vz_m2z, vz[c - L], vz[c], vz[c + L]), g.rdz);
-    const float l = __ldg(f.lam + c), m = __ldg(f.mu + c);
-    const float l2m = fadd(l, fmul(2.0f, m));
-    float sxx = fadd(f.sxx[c], fmul(g.dt, fadd(fmul(l2m, ex), fmul(l, ez))));
-    float szz = fadd(f.szz[c], fmul(g.dt, fadd(fmul(l, ex), fmul(l2m, ez))));
-    const float gx = fmul(el_dfwd(vz[c - 1], vz[c], vz[c + 1], vz[c + 2]), g.rdx);
-    const float hz = fmul(el_dfwd(vx[c - L], vx[c], vx[c + L], vx[c + 2 * L]), g.rdz);
-    float sxz = fadd(f.sxz[c], fmul(fmul(g.dt, m), fadd(gx, hz)));
-    if (g.sponge) {
-        const float s = __ldg(g.sponge + c);
-        sxx = fmul(sxx, s);
-        szz = fmul(szz, s);
-        sxz = fmul(sxz, s);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (ixb + j >= g.ldx) continue;
+        if (el_in_m(ixb + j, iz, g.nx, g.nz, g.free_surface)) dst[off + j] = u[j];
+        else if (!in_place) dst[off + j] = src[off + j];
     }
-    f.sxx[c] = sxx;
-    f.szz[c] = szz;
-    f.sxz[c] = sxz;
 }
 
-inline void launch_elastic_step(const ElGeom& g, const ElFields& f, cudaStream_t st)
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32)
+    elastic_velocity_kernel(const __grid_constant__ ElMaps maps, const ElGeom g, const ElStep s)
 {
-    dim3 block(32, 8);
-    dim3 grid((g.nx + 31) / 32, (g.nz + 7) / 8);
-    elastic_velocity_kernel<<<grid, block, 0, st>>>(g, f);
-    elastic_stress_kernel<<<grid, block, 0, st>>>(g, f);
+    using T = ElTile<WARPS, RPW>;
+    extern __shared__ __align__(128) float smem[];
+    float* bxx = smem;             // sxx box
+    float* bxz = smem + T::BOX;    // sxz box
+    float* bzz = smem + 2 * T::BOX;  // szz box
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 3 * T::BOX);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ;
+    if (tid == 0) {
+        prefetch_tensormap(&maps.src);
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(bar, 3u * T::BOX * 4u);
+        tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, EL_SXX, bar);
+        tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, EL_SXZ, bar);
+        tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, EL_SZZ, bar);
+    }
+    __syncthreads();
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    // every lane takes part in the shuffles; lanes past the row pitch only skip
+    // their loads and stores
+    const int ixb = x0 + 4 * lane;
+    const bool col_ok = ixb < g.ldx;
+    const bool in_place = s.src == s.dst;
+    const float* vx_s = s.src + (size_t)EL_VX * s.plane;
+    const float* vz_s = s.src + (size_t)EL_VZ * s.plane;
+    float* vx_d = s.dst + (size_t)EL_VX * s.plane;
+    float* vz_d = s.dst + (size_t)EL_VZ * s.plane;
+    const float inj = s.inj_w ? fmul(__ldg(s.inj_w), g.dt) : 0.0f;
+    const int zr0 = z0 + warp * RPW;
+    const int sr = zr0 - (z0 - 2);  // box row of global row zr0
+    // z windows: sxz rows z-2..z+1, szz rows z-1..z+2
+    float4 xz0 = el_row4(bxz, sr - 2, lane), xz1 = el_row4(bxz, sr - 1, lane),
+           xz2 = el_row4(bxz, sr, lane);
+    float4 zz0 = el_row4(bzz, sr - 1, lane), zz1 = el_row4(bzz, sr, lane),
+           zz2 = el_row4(bzz, sr + 1, lane);
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int iz = zr0 + r;
+        const float4 xz3 = el_row4(bxz, sr + r + 1, lane);
+        const float4 zz3 = el_row4(bzz, sr + r + 2, lane);
+        float exx[8], exz[8];
+        el_xrow(bxx, sr + r, lane, exx);
+        el_xrow(bxz, sr + r, lane, exz);
+        if (iz < g.nz && col_ok) {
+            const size_t off = (size_t)iz * g.ldx + ixb;
+            const float4 vx4 = __ldg(reinterpret_cast<const float4*>(vx_s + off));
+            float4 vz4 = __ldg(reinterpret_cast<const float4*>(vz_s + off));
+            const float4 bx4 = __ldg(reinterpret_cast<const float4*>(s.bx + off));
+            const float4 bz4 = __ldg(reinterpret_cast<const float4*>(s.bz + off));
+            const float4 sp4 = g.sponge ? __ldg(reinterpret_cast<const float4*>(g.sponge + off))
+                                        : make_float4(1.f, 1.f, 1.f, 1.f);
+            float ux[4], uz[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float vz_in = el_c(vz4, j);
+                if (s.inj_w && iz == s.inj_iz && ixb + j == s.inj_ix) vz_in = fadd(vz_in, inj);
+                const float a = fmul(el_dfwd(exx[j + 1], exx[j + 2], exx[j + 3], exx[j + 4]), g.rdx);
+                const float b = fmul(el_dbwd(el_c(xz0, j), el_c(xz1, j), el_c(xz2, j), el_c(xz3, j)),
+                                     g.rdz);
+                float vx = fadd(el_c(vx4, j), fmul(fmul(g.dt, el_c(bx4, j)), fadd(a, b)));
+                const float e = fmul(el_dbwd(exz[j], exz[j + 1], exz[j + 2], exz[j + 3]), g.rdx);
+                const float h = fmul(el_dfwd(el_c(zz0, j), el_c(zz1, j), el_c(zz2, j), el_c(zz3, j)),
+                                     g.rdz);
+                float vz = fadd(vz_in, fmul(fmul(g.dt, el_c(bz4, j)), fadd(e, h)));
+                if (g.sponge) {
+                    vx = fmul(vx, el_c(sp4, j));
+                    vz = fmul(vz, el_c(sp4, j));
+                }
+                ux[j] = vx;
+                uz[j] = vz;
+            }
+            // (the source term is only used on cells of M)
+            el_store_row(vx_d, vx_s, off, ixb, iz, g, ux, in_place);
+            el_store_row(vz_d, vz_s, off, ixb, iz, g, uz, in_place);
+        }
+        xz0 = xz1;
+        xz1 = xz2;
+        xz2 = xz3;
+        zz0 = zz1;
+        zz1 = zz2;
+        zz2 = zz3;
+    }
+}
+
+template <int WARPS, int RPW>
+__global__ void __launch_bounds__(WARPS * 32)
+    elastic_stress_kernel(const __grid_constant__ ElMaps maps, const ElGeom g, const ElStep s)
+{
+    using T = ElTile<WARPS, RPW>;
+    extern __shared__ __align__(128) float smem[];
+    float* bvx = smem;
+    float* bvz = smem + T::BOX;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::BOX);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ;
+    if (tid == 0) {
+        prefetch_tensormap(&maps.dst);
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(bar, 2u * T::BOX * 4u);
+        tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, EL_VX, bar);
+        tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, EL_VZ, bar);
+    }
+    __syncthreads();
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    const int ixb = x0 + 4 * lane;
+    const bool col_ok = ixb < g.ldx;  // see the velocity phase
+    const bool in_place = s.src == s.dst;
+    const float* sxx_s = s.src + (size_t)EL_SXX * s.plane;
+    const float* szz_s = s.src + (size_t)EL_SZZ * s.plane;
+    const float* sxz_s = s.src + (size_t)EL_SXZ * s.plane;
+    float* sxx_d = s.dst + (size_t)EL_SXX * s.plane;
+    float* szz_d = s.dst + (size_t)EL_SZZ * s.plane;
+    float* sxz_d = s.dst + (size_t)EL_SXZ * s.plane;
+    const int zr0 = z0 + warp * RPW;
+    const int sr = zr0 - (z0 - 2);
+    // z windows: vx rows z-1..z+2, vz rows z-2..z+1
+    float4 x0w = el_row4(bvx, sr - 1, lane), x1w = el_row4(bvx, sr, lane),
+           x2w = el_row4(bvx, sr + 1, lane);
+    float4 z0w = el_row4(bvz, sr - 2, lane), z1w = el_row4(bvz, sr - 1, lane),
+           z2w = el_row4(bvz, sr, lane);
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int iz = zr0 + r;
+        const float4 x3w = el_row4(bvx, sr + r + 2, lane);
+        const float4 z3w = el_row4(bvz, sr + r + 1, lane);
+        float evx[8], evz[8];
+        el_xrow(bvx, sr + r, lane, evx);
+        el_xrow(bvz, sr + r, lane, evz);
+        if (iz < g.nz && col_ok) {
+            const size_t off = (size_t)iz * g.ldx + ixb;
+            const float4 lam4 = __ldg(reinterpret_cast<const float4*>(s.lam + off));
+            const float4 mu4 = __ldg(reinterpret_cast<const float4*>(s.mu + off));
+            const float4 sxx4 = __ldg(reinterpret_cast<const float4*>(sxx_s + off));
+            const float4 szz4 = __ldg(reinterpret_cast<const float4*>(szz_s + off));
+            const float4 sxz4 = __ldg(reinterpret_cast<const float4*>(sxz_s + off));
+            const float4 sp4 = g.sponge ? __ldg(reinterpret_cast<const float4*>(g.sponge + off))
+                                        : make_float4(1.f, 1.f, 1.f, 1.f);
+            float uxx[4], uzz[4], uxz[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int ix = ixb + j;
+                const float l = el_c(lam4, j), m = el_c(mu4, j);
+                const float ex = fmul(el_dbwd(evx[j], evx[j + 1], evx[j + 2], evx[j + 3]), g.rdx);
+                uxx[j] = el_c(sxx4, j);
+                uzz[j] = el_c(szz4, j);
+                uxz[j] = el_c(sxz4, j);
+                if (g.free_surface && iz == 0) {
+                    // free-surface row (wave2d.c:198-211)
+                    uzz[j] = 0.0f;
+                    uxz[j] = 0.0f;
+                    if (ix >= 2 && ix < g.nx - 2) {
+                        const float num = fmul(fmul(4.0f, m), fadd(l, m));
+                        const float den = fadd(fadd(l, fmul(2.0f, m)), 1e-8f);
+                        uxx[j] = fmul(__fdiv_rn(num, den), ex);
+                    }
+                    continue;
+                }
+                if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) continue;
+                const float ez = fmul(el_dbwd(el_c(z0w, j), el_c(z1w, j), el_c(z2w, j), el_c(z3w, j)),
+                                      g.rdz);
+                const float l2m = fadd(l, fmul(2.0f, m));
+                float sxx = fadd(uxx[j], fmul(g.dt, fadd(fmul(l2m, ex), fmul(l, ez))));
+                float szz = fadd(uzz[j], fmul(g.dt, fadd(fmul(l, ex), fmul(l2m, ez))));
+                const float gx = fmul(el_dfwd(evz[j + 1], evz[j + 2], evz[j + 3], evz[j + 4]), g.rdx);
+                const float hz = fmul(el_dfwd(el_c(x0w, j), el_c(x1w, j), el_c(x2w, j), el_c(x3w, j)),
+                                      g.rdz);
+                float sxz = fadd(uxz[j], fmul(fmul(g.dt, m), fadd(gx, hz)));
+                if (g.sponge) {
+                    const float sp = el_c(sp4, j);
+                    sxx = fmul(sxx, sp);
+                    szz = fmul(szz, sp);
+                    sxz = fmul(sxz, sp);
+                }
+                uxx[j] = sxx;
+                uzz[j] = szz;
+                uxz[j] = sxz;
+            }
+            bool all = true;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) all &= el_in_m(ixb + j, iz, g.nx, g.nz, g.free_surface);
+            if (all) {
+                *reinterpret_cast<float4*>(sxx_d + off) = make_float4(uxx[0], uxx[1], uxx[2], uxx[3]);
+                *reinterpret_cast<float4*>(szz_d + off) = make_float4(uzz[0], uzz[1], uzz[2], uzz[3]);
+                *reinterpret_cast<float4*>(sxz_d + off) = make_float4(uxz[0], uxz[1], uxz[2], uxz[3]);
+            } else {
+                const bool fs_row = g.free_surface && iz == 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int ix = ixb + j;
+                    if (ix >= g.ldx) continue;
+                    // written: M, the free-surface row inside the grid, and (out of
+                    // place) every other cell as a copy
+                    const bool w = el_in_m(ix, iz, g.nx, g.nz, g.free_surface) ||
+                                   (fs_row && ix < g.nx) || !in_place;
+                    if (!w) continue;
+                    sxx_d[off + j] = uxx[j];
+                    szz_d[off + j] = uzz[j];
+                    sxz_d[off + j] = uxz[j];
+                }
+            }
+        }
+        x0w = x1w;
+        x1w = x2w;
+        x2w = x3w;
+        z0w = z1w;
+        z1w = z2w;
+        z2w = z3w;
+    }
+}
+
+constexpr int EL_WARPS = 4, EL_RPW = 4;
+
+// The 3D tensor map of a 5-plane state for these kernels.
+inline int make_el_state_map(CUtensorMap* m, const float* base, int nx, int nz, int ldx,
+                             size_t plane)
+{
+    return make_tensor_map_3d(m, base, nx, nz, 5, ldx, plane, EL_SW,
+                              ElTile<EL_WARPS, EL_RPW>::TZ + 4);
+}
+
+// Velocity then stress phase of one step (src -> dst; src == dst updates in place).
+inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, const ElStep& s,
+                                       cudaStream_t st)
+{
+    using T = ElTile<EL_WARPS, EL_RPW>;
+    const int vbytes = 3 * T::BOX * 4 + 128, sbytes = 2 * T::BOX * 4 + 128;
+    static bool attr_set = false;  // one attribute call per process
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(elastic_velocity_kernel<EL_WARPS, EL_RPW>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, vbytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(elastic_stress_kernel<EL_WARPS, EL_RPW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ);
+    elastic_velocity_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, vbytes, st>>>(maps, g, s);
+    ElStep s2 = s;
+    s2.inj_w = nullptr;
+    elastic_stress_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, sbytes, st>>>(maps, g, s2);
+    return cudaGetLastError();
 }
 
 }  // namespace w2d

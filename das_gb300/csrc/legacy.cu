@@ -208,9 +208,31 @@ int legacy_elastic(float* vx, float* vz, float* sxx, float* szz, float* sxz, con
     geo.dt = dt;
     geo.free_surface = fs ? 1 : 0;
     geo.sponge = sponge ? d[9] : nullptr;
-    ElFields f{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]};
-    launch_elastic_step(geo, f, g.st);
-    W2D_CUDA_TRY(cudaGetLastError());
+    ElMaps maps;
+    if ((rc = make_el_state_map(&maps.src, d[0], nx, nz, ldx, plane))) return rc;
+    maps.dst = maps.src;
+    ElStep st;
+    st.src = d[0];
+    st.dst = d[0];
+    st.plane = plane;
+    st.lam = d[5];
+    st.mu = d[6];
+    st.bx = d[7];
+    st.bz = d[8];
+    st.inj_ix = st.inj_iz = -1;
+    st.inj_w = nullptr;
+    st.err = g.err;
+    W2D_CUDA_TRY(launch_elastic_step(geo, maps, st, g.st));
+    {
+        unsigned h = 0;
+        W2D_CUDA_TRY(cudaMemcpyAsync(&h, g.err, 4, cudaMemcpyDeviceToHost, g.st));
+        W2D_CUDA_TRY(cudaStreamSynchronize(g.st));
+        if (h) {
+            cudaMemsetAsync(g.err, 0, 4, g.st);
+            set_error("device wait gave up in elastic_2d_step");
+            return W2D_ETIMEOUT;
+        }
+    }
     float* outs[5] = {vx, vz, sxx, szz, sxz};
     int slots[5] = {0, 1, 2, 3, 4};
     for (int i = 0; i < 5; ++i)

@@ -134,6 +134,17 @@ __device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* m
         : "memory");
 }
 
+// 3D tiled TMA load (x, row, plane) of one box into shared memory.
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // L2 eviction-priority policies for cache-hinted loads and stores.
 __device__ __forceinline__ uint64_t policy_evict_last()
 {
@@ -199,5 +210,9 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 // outside [0,nx) x [0,nz) return zero.
 int make_tensor_map_2d(CUtensorMap* out, const float* base, int nx, int nz, int ldx, int box_x,
                        int box_z);
+// Tensor map over n_planes consecutive pitched planes (plane stride in floats):
+// dims (nx, nz, n_planes), box (box_x, box_z, 1).
+int make_tensor_map_3d(CUtensorMap* out, const float* base, int nx, int nz, int n_planes, int ldx,
+                       size_t plane_stride, int box_x, int box_z);
 
 }  // namespace w2d
