@@ -438,9 +438,8 @@ def run_batched(args, dist):
 def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
     """Poisson arrivals at `rate` jobs/s; grid sides log-uniform from 128 x 256 to
     1024 x 4096 (times side_scale), nt uniform in [1000, 8000] (times nt_scale), 1-32
-    shots per job sharing the job's smoothed faulted model; 80 % acoustic / 20 % elastic.
-    An elastic shot costs about ten acoustic ones (five fields, gradient with
-    recomputation), so elastic jobs get half the grid sides and 1-4 shots."""
+    shots per job sharing the job's smoothed faulted model; 80 % acoustic / 20 % elastic
+    (the same size distribution for both kinds)."""
     from das_gb300.batch import ShotJob
     from das_gb300.serving import poisson_trace
     from das_gb300.synthetic import _layered_faulted
@@ -452,8 +451,6 @@ def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
         nx = int(np.exp(rng.uniform(np.log(256), np.log(4096))) * side_scale)
         nt = max(64, int(rng.integers(1000, 8001) * nt_scale))
         kind = "elastic" if rng.uniform() < 0.2 else "acoustic"
-        if kind == "elastic":
-            nz, nx = nz // 2, nx // 2
         nz, nx = max(nz, 48), max(nx, 96)
         d = 5.0
         zmax = (nz - 1) * d
@@ -463,7 +460,7 @@ def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
         v = gaussian_filter(v, 3.0).astype(np.float32)
         dt = 5e-4
         w, _ = ricker_wavelet(float(rng.uniform(3.0, 5.0)), dt, nt * dt)
-        n_sh = int(rng.integers(1, 33)) if kind == "acoustic" else int(rng.integers(1, 5))
+        n_sh = int(rng.integers(1, 33))
         if kind == "elastic":
             # shear velocity from the same model; vertical-strain observations
             vs = (v / 1.73).astype(np.float32)  # vp = 1.73 vs = v: same CFL as the acoustic
@@ -549,16 +546,19 @@ def run_served(args, dist):
                           args.serve_nt_scale)
     n_el = sum(r.kind == "elastic" for r in trace)
     tile = tuple(int(t) for t in (args.tile or "4,4").split(","))
-    eng = BatchEngine(arena_bytes=int(args.arena_gb * (1 << 30)), max_shots=4096, tile=tile,
-                      steps_per_launch=args.spl, launches_per_graph=args.lpg,
+    # the elastic workers hold up to ~17 GB each (checkpoints and one recomputed segment
+    # of a 1024 x 4096, nt 8000 grid): leave them room beside the acoustic arena
+    eng = BatchEngine(arena_bytes=int(min(args.arena_gb, 160.0) * (1 << 30)), max_shots=4096,
+                      tile=tile, steps_per_launch=args.spl, launches_per_graph=args.lpg,
                       form=args.batch_form)
-    from das_gb300.elastic import ElasticExecutor
+    from das_gb300.elastic import ElasticExecutor, ElasticSolver2D
     eng.run([s for r in trace if r.kind == "acoustic" for s in r.shots][:1])  # graph capture
     ex = ElasticExecutor()
     out, st = RTMServer(eng, elastic_executor=ex).serve(trace, realtime=True)
     eng.close()
-    # plain per-shot loop over the first jobs of the same trace, arrivals on the wall clock
-    m = min(args.plain_jobs, len(trace))
+    # plain per-shot loop over the same trace (or its first --plain-jobs jobs), FIFO,
+    # arrivals on the wall clock
+    m = len(trace) if args.plain_jobs <= 0 else min(args.plain_jobs, len(trace))
     t0 = time.perf_counter()
     lat, shots_done = [], 0
     for r in trace[:m]:
@@ -567,10 +567,12 @@ def run_served(args, dist):
             time.sleep(wait)
         j0 = r.shots[0]
         if r.kind == "elastic":
-            es = ex._solver(j0)
+            es = ElasticSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha,
+                                 j0.free_surface_top)
             for j in r.shots:
                 ex.migrate_shot(es, j)
                 shots_done += 1
+            es.close()
         else:
             s = WaveSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha, True)
             e = TSWRTMEngine(s, "all")
@@ -586,13 +588,13 @@ def run_served(args, dist):
     plain = {"jobs": m, "shots": shots_done, "shots_per_s": shots_done / plain_span,
              "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
     served_first = [x.latency for x in out[:m]]
+    plain["makespan_s"] = plain_span
     out_line = {"metric": "served RTM shots/s", "value": st["shots_per_s"], "unit": "shots/s",
                 "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": f"Poisson trace of {len(trace)} jobs at {args.serve_rate} "
                                        f"jobs/s, sides log-uniform 128x256..1024x4096 x "
                                        f"{args.serve_side_scale}, nt U[1000,8000] x "
-                                       f"{args.serve_nt_scale}, 1-32 shots/job; elastic "
-                                       f"jobs half the sides, 1-4 shots",
+                                       f"{args.serve_nt_scale}, 1-32 shots/job",
                            "elastic_jobs_in_trace": n_el, "tile": list(tile),
                            "form": args.batch_form,
                            "steps_per_launch": args.spl, "launches_per_graph": args.lpg},
@@ -685,7 +687,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)
     ap.add_argument("--serve-nt-scale", type=float, default=1.0)
-    ap.add_argument("--plain-jobs", type=int, default=8)
+    ap.add_argument("--plain-jobs", type=int, default=0)  # 0: the whole trace
     ap.add_argument("--batch-shots", type=int, default=256)
     ap.add_argument("--batch-nt-scale", type=float, default=1.0)
     ap.add_argument("--plain-shots", type=int, default=16)

@@ -21,6 +21,8 @@
 //   K3  g_bx += s dt adj_vx (Dx+ sxx_n + Dz- sxz_n), g_bz likewise (forward stresses of u_n);
 //       adj_v = s adj_v;  r = dt b adj_v
 //   K4  adj_sigma = q + G^T r = q - (Dx- rx,  Dz- rz,  Dz+ rx + Dx+ rz)
+// K2 and K3 run as one kernel (el_adj_k23), and K1 of step n-1 runs inside K4 of
+// step n (el_adj_k4), so one adjoint step is three passes.
 // Receiver residuals enter as adj_vz += Dz-^T (residual) on the four cells of
 // the receiver's stencil.  Float32; not bit-for-bit with anything, checked
 // against finite differences.
@@ -93,52 +95,64 @@ static __global__ void el_adj_k1(ElGeom g, ElParams p, ElState a, ElState t)
     t.sxz[c] = g.dt * m * qxz;
 }
 
-// K2 (fwd: forward velocities of u_{n+1})
-static __global__ void el_adj_k2(ElGeom g, ElParams p, ElState a, ElState t, ElState fwd,
-                                 float* g_lam, float* g_mu)
+// K2 and K3 of one step in one pass: K3 touches the adjoint velocities only at
+// their own cell, right after K2 has produced them.
+static __global__ void el_adj_k23(ElGeom g, ElParams p, ElState a, ElState t, ElState r,
+                                  ElState f_next, ElState f_curr, float* g_lam, float* g_mu,
+                                  float* g_bx, float* g_bz)
 {
     EL_CELL
-    (void)sp;
     const int nx = g.nx, nz = g.nz;
-    a.vx[c] -= d_fwd_x(t.sxx, ix, iz, nx, nz, L) * g.rdx + d_bwd_z(t.sxz, ix, iz, nx, nz, L) * g.rdz;
-    a.vz[c] -= d_fwd_z(t.szz, ix, iz, nx, nz, L) * g.rdz + d_bwd_x(t.sxz, ix, iz, nx, nz, L) * g.rdx;
-    const float exx = d_bwd_x(fwd.vx, ix, iz, nx, nz, L) * g.rdx;
-    const float ezz = d_bwd_z(fwd.vz, ix, iz, nx, nz, L) * g.rdz;
-    const float exz = d_fwd_x(fwd.vz, ix, iz, nx, nz, L) * g.rdx +
-                      d_fwd_z(fwd.vx, ix, iz, nx, nz, L) * g.rdz;
+    // K2
+    float avx = a.vx[c], avz = a.vz[c];
+    avx -= d_fwd_x(t.sxx, ix, iz, nx, nz, L) * g.rdx + d_bwd_z(t.sxz, ix, iz, nx, nz, L) * g.rdz;
+    avz -= d_fwd_z(t.szz, ix, iz, nx, nz, L) * g.rdz + d_bwd_x(t.sxz, ix, iz, nx, nz, L) * g.rdx;
+    const float exx = d_bwd_x(f_next.vx, ix, iz, nx, nz, L) * g.rdx;
+    const float ezz = d_bwd_z(f_next.vz, ix, iz, nx, nz, L) * g.rdz;
+    const float exz = d_fwd_x(f_next.vz, ix, iz, nx, nz, L) * g.rdx +
+                      d_fwd_z(f_next.vx, ix, iz, nx, nz, L) * g.rdz;
     const float qxx = a.sxx[c], qzz = a.szz[c], qxz = a.sxz[c];
     g_lam[c] += g.dt * (exx + ezz) * (qxx + qzz);
     g_mu[c] += g.dt * (2.0f * exx * qxx + 2.0f * ezz * qzz + exz * qxz);
-}
-
-// K3 (fwd: forward stresses of u_n)
-static __global__ void el_adj_k3(ElGeom g, ElParams p, ElState a, ElState r, ElState fwd,
-                                 float* g_bx, float* g_bz)
-{
-    EL_CELL
-    const int nx = g.nx, nz = g.nz;
-    const float gx = d_fwd_x(fwd.sxx, ix, iz, nx, nz, L) * g.rdx +
-                     d_bwd_z(fwd.sxz, ix, iz, nx, nz, L) * g.rdz;
-    const float gz = d_bwd_x(fwd.sxz, ix, iz, nx, nz, L) * g.rdx +
-                     d_fwd_z(fwd.szz, ix, iz, nx, nz, L) * g.rdz;
-    g_bx[c] += sp * g.dt * a.vx[c] * gx;
-    g_bz[c] += sp * g.dt * a.vz[c] * gz;
-    const float vx = sp * a.vx[c], vz = sp * a.vz[c];
+    // K3
+    const float gx = d_fwd_x(f_curr.sxx, ix, iz, nx, nz, L) * g.rdx +
+                     d_bwd_z(f_curr.sxz, ix, iz, nx, nz, L) * g.rdz;
+    const float gz = d_bwd_x(f_curr.sxz, ix, iz, nx, nz, L) * g.rdx +
+                     d_fwd_z(f_curr.szz, ix, iz, nx, nz, L) * g.rdz;
+    g_bx[c] += sp * g.dt * avx * gx;
+    g_bz[c] += sp * g.dt * avz * gz;
+    const float vx = sp * avx, vz = sp * avz;
     a.vx[c] = vx;
     a.vz[c] = vz;
     r.vx[c] = g.dt * p.bx[c] * vx;
     r.vz[c] = g.dt * p.bz[c] * vz;
 }
 
-// K4
-static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r)
+// K4 of step n, followed (then_k1) by K1 of step n-1 on the same cell: K1 reads
+// only this cell's adjoint stresses, which K4 has just produced, so the two fuse
+// into one pass (the receiver residual added between them touches vz only).
+static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r, ElState t,
+                                 int then_k1)
 {
     EL_CELL
-    (void)sp;
     const int nx = g.nx, nz = g.nz;
-    a.sxx[c] -= d_bwd_x(r.vx, ix, iz, nx, nz, L) * g.rdx;
-    a.szz[c] -= d_bwd_z(r.vz, ix, iz, nx, nz, L) * g.rdz;
-    a.sxz[c] -= d_fwd_z(r.vx, ix, iz, nx, nz, L) * g.rdz + d_fwd_x(r.vz, ix, iz, nx, nz, L) * g.rdx;
+    float sxx = a.sxx[c], szz = a.szz[c], sxz = a.sxz[c];
+    sxx -= d_bwd_x(r.vx, ix, iz, nx, nz, L) * g.rdx;
+    szz -= d_bwd_z(r.vz, ix, iz, nx, nz, L) * g.rdz;
+    sxz -= d_fwd_z(r.vx, ix, iz, nx, nz, L) * g.rdz + d_fwd_x(r.vz, ix, iz, nx, nz, L) * g.rdx;
+    if (then_k1) {
+        const float qxx = sp * sxx, qzz = sp * szz, qxz = sp * sxz;
+        sxx = qxx;
+        szz = qzz;
+        sxz = qxz;
+        const float l = p.lam[c], m = p.mu[c];
+        t.sxx[c] = g.dt * ((l + 2.0f * m) * qxx + l * qzz);
+        t.szz[c] = g.dt * (l * qxx + (l + 2.0f * m) * qzz);
+        t.sxz[c] = g.dt * m * qxz;
+    }
+    a.sxx[c] = sxx;
+    a.szz[c] = szz;
+    a.sxz[c] = sxz;
 }
 
 // Vertical-strain receivers of u_{n+1} (the source term is added by the step's

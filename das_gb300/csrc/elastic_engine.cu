@@ -294,6 +294,8 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
     const int rb = (e->nx + 127) / 128;
     el_adj_receivers<<<rb, 128, 0, e->st>>>(g, a.vz, e->rec_ptr, e->rec_list, e->rec_iz,
                                             e->traces + (size_t)(nt - 1) * n_rec);
+    // K1 of the last step; every later K1 runs inside the K4 of the step after it
+    el_adj_k1<<<grd, blk, 0, e->st>>>(g, prm, a, t);
     for (int sgi = e->n_seg - 1; sgi >= 0; --sgi) {
         const int a0 = sgi * e->seg_len, b0 = std::min(nt, a0 + e->seg_len);
         // recompute u_a0 .. u_b0 into the segment buffer
@@ -311,10 +313,9 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
         for (int n = b0 - 1; n >= a0; --n) {
             ElState f_next = e->S(e->seg + (size_t)(n + 1 - a0) * 5 * P);  // u_{n+1}
             ElState f_curr = e->S(e->seg + (size_t)(n - a0) * 5 * P);      // u_n
-            el_adj_k1<<<grd, blk, 0, e->st>>>(g, prm, a, t);
-            el_adj_k2<<<grd, blk, 0, e->st>>>(g, prm, a, t, f_next, glam, gmu);
-            el_adj_k3<<<grd, blk, 0, e->st>>>(g, prm, a, r, f_curr, gbx, gbz);
-            el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, a, r);
+            el_adj_k23<<<grd, blk, 0, e->st>>>(g, prm, a, t, r, f_next, f_curr, glam, gmu, gbx,
+                                               gbz);
+            el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, a, r, t, n >= 1 ? 1 : 0);
             if (n >= 1)
                 el_adj_receivers<<<rb, 128, 0, e->st>>>(g, a.vz, e->rec_ptr, e->rec_list,
                                                         e->rec_iz,

@@ -102,24 +102,35 @@ def elastic_traces(vs: torch.Tensor, solver: ElasticSolver2D, wavelet, source_ix
 
 
 class ElasticExecutor:
-    """Runs elastic migration jobs on a worker thread with its own CUDA stream, so
-    they overlap the acoustic batch on the device.  A job's shots carry the shear
-    velocity in ``vel_fwd`` and observed vertical-strain traces in ``data``; each
-    shot's result is (dJ/dvs, None) for J = 0.5 * ||d(vs) - data||^2."""
+    """Runs elastic migration jobs on worker threads, each with its own CUDA stream, so
+    they overlap each other and the acoustic batch on the device.  A job's shots carry
+    the shear velocity in ``vel_fwd`` and observed vertical-strain traces in ``data``;
+    each shot's result is (dJ/dvs, None) for J = 0.5 * ||d(vs) - data||^2.  Shots are
+    the unit of work (a job's shots spread over the workers); a worker keeps the solver
+    of the grid it ran last and drops it when the grid changes, so device memory holds
+    at most one elastic engine per worker."""
 
-    def __init__(self):
+    def __init__(self, workers: int = 3):
         import queue
         import threading
         self._q = queue.Queue()
         self._done = []
         self._lock = threading.Lock()
         self._pending = 0
+        self._jobs = {}  # job_id -> [request, results, shots left]
         self._solvers = {}
-        self._t = threading.Thread(target=self._loop, daemon=True)
-        self._t.start()
+        self._threads = [threading.Thread(target=self._loop, daemon=True)
+                         for _ in range(max(1, int(workers)))]
+        for t in self._threads:
+            t.start()
+
+    @staticmethod
+    def _key(s):
+        return (s.nx, s.nz, s.dx, s.dz, s.dt, s.n_sponge, s.sponge_alpha, s.free_surface_top)
 
     def _solver(self, s):
-        key = (s.nx, s.nz, s.dx, s.dz, s.dt, s.n_sponge, s.sponge_alpha, s.free_surface_top)
+        """A solver for shot s kept by the calling thread's caller (used outside the workers)."""
+        key = self._key(s)
         if key not in self._solvers:
             self._solvers[key] = ElasticSolver2D(s.nx, s.nz, s.dx, s.dz, s.dt, s.n_sponge,
                                                  s.sponge_alpha, s.free_surface_top)
@@ -138,19 +149,39 @@ class ElasticExecutor:
     def _loop(self):
         import time
         torch.cuda.set_stream(torch.cuda.Stream())
+        key, solver = None, None
         while True:
-            req = self._q.get()
-            if req is None:
+            item = self._q.get()
+            if item is None:
+                if solver is not None:
+                    solver.close()
                 return
-            res = [self.migrate_shot(self._solver(s), s) for s in req.shots]
+            jid, k = item
             with self._lock:
-                self._done.append((req.job_id, res, time.perf_counter()))
-                self._pending -= 1
+                req = self._jobs[jid][0]
+            shot = req.shots[k]
+            if self._key(shot) != key:
+                if solver is not None:
+                    solver.close()
+                key = self._key(shot)
+                solver = ElasticSolver2D(shot.nx, shot.nz, shot.dx, shot.dz, shot.dt,
+                                         shot.n_sponge, shot.sponge_alpha, shot.free_surface_top)
+            res = self.migrate_shot(solver, shot)
+            with self._lock:
+                entry = self._jobs[jid]
+                entry[1][k] = res
+                entry[2] -= 1
+                if entry[2] == 0:
+                    self._done.append((jid, entry[1], time.perf_counter()))
+                    del self._jobs[jid]
+                    self._pending -= 1
 
     def submit(self, req):
         with self._lock:
             self._pending += 1
-        self._q.put(req)
+            self._jobs[req.job_id] = [req, [None] * len(req.shots), len(req.shots)]
+        for k in range(len(req.shots)):
+            self._q.put((req.job_id, k))
 
     def pending(self) -> int:
         with self._lock:
@@ -162,5 +193,10 @@ class ElasticExecutor:
         return out
 
     def close(self):
-        self._q.put(None)
-        self._t.join()
+        for _ in self._threads:
+            self._q.put(None)
+        for t in self._threads:
+            t.join()
+        for sv in self._solvers.values():
+            sv.close()
+        self._solvers = {}
