@@ -79,6 +79,12 @@ _SIGS = {
                                                       c_void_p]),
     "w2d_elastic_gradient": (c_int, [c_void_p] * 6),
     "w2d_elastic_last_ms": (c_float, [c_void_p]),
+    "w2d_elastic_forward_batch": (c_int, [c_void_p, c_int] + [c_void_p] * 5 + [c_int, c_void_p,
+                                                                              c_void_p, c_void_p,
+                                                                              c_int, c_int,
+                                                                              c_void_p]),
+    "w2d_elastic_gradient_batch": (c_int, [c_void_p] * 6),
+    "w2d_elastic_shot_bytes": (c_ull, [c_int, c_int, c_int, c_int]),
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),

@@ -36,6 +36,17 @@ struct ElState {
     float *vx, *vz, *sxx, *szz, *sxz;
 };
 
+__device__ __forceinline__ ElState el_shift(ElState s, size_t o)
+{
+    return ElState{s.vx + o, s.vz + o, s.sxx + o, s.szz + o, s.sxz + o};
+}
+
+// Per-shot strides (floats) of a batch: shot s of a state at + s * state, of the
+// parameters at + s * param, of the four gradient planes at + s * grad.
+struct ElStrides {
+    size_t state, param, grad;
+};
+
 struct ElParams {
     const float *lam, *mu, *bx, *bz;
     const float* sponge;  // pitched, or null
@@ -73,23 +84,32 @@ __device__ __forceinline__ float d_bwd_z(const float* a, int ix, int iz, int nx,
            k2 * (el_at(a, ix, iz + 1, nx, nz, L) - el_at(a, ix, iz - 2, nx, nz, L));
 }
 
+// one cell of M of shot blockIdx.z; c indexes the cell within a plane of that shot
 #define EL_CELL                                                  \
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;        \
     const int iz = blockIdx.y * blockDim.y + threadIdx.y;        \
     if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) return;    \
     const int L = g.ldx;                                         \
     const size_t c = (size_t)iz * L + ix;                        \
-    const float sp = p.sponge ? p.sponge[c] : 1.0f;
+    const size_t po_ = blockIdx.z * sd.param;                    \
+    const float sp = p.sponge ? p.sponge[c] : 1.0f;              \
+    const float* lam_ = p.lam + po_;                             \
+    const float* mu_ = p.mu + po_;                               \
+    const float* bx_ = p.bx + po_;                               \
+    const float* bz_ = p.bz + po_;                               \
+    (void)lam_; (void)mu_; (void)bx_; (void)bz_;
 
 // K1
-static __global__ void el_adj_k1(ElGeom g, ElParams p, ElState a, ElState t)
+static __global__ void el_adj_k1(ElGeom g, ElParams p, ElStrides sd, ElState a, ElState t)
 {
     EL_CELL
+    a = el_shift(a, blockIdx.z * sd.state);
+    t = el_shift(t, blockIdx.z * sd.state);
     const float qxx = sp * a.sxx[c], qzz = sp * a.szz[c], qxz = sp * a.sxz[c];
     a.sxx[c] = qxx;
     a.szz[c] = qzz;
     a.sxz[c] = qxz;
-    const float l = p.lam[c], m = p.mu[c];
+    const float l = lam_[c], m = mu_[c];
     t.sxx[c] = g.dt * ((l + 2.0f * m) * qxx + l * qzz);
     t.szz[c] = g.dt * (l * qxx + (l + 2.0f * m) * qzz);
     t.sxz[c] = g.dt * m * qxz;
@@ -97,12 +117,22 @@ static __global__ void el_adj_k1(ElGeom g, ElParams p, ElState a, ElState t)
 
 // K2 and K3 of one step in one pass: K3 touches the adjoint velocities only at
 // their own cell, right after K2 has produced them.
-static __global__ void el_adj_k23(ElGeom g, ElParams p, ElState a, ElState t, ElState r,
-                                  ElState f_next, ElState f_curr, float* g_lam, float* g_mu,
-                                  float* g_bx, float* g_bz)
+static __global__ void el_adj_k23(ElGeom g, ElParams p, ElStrides sd, ElState a, ElState t,
+                                  ElState r, ElState f_next, ElState f_curr, float* g_lam,
+                                  float* g_mu, float* g_bx, float* g_bz)
 {
     EL_CELL
     const int nx = g.nx, nz = g.nz;
+    const size_t so = blockIdx.z * sd.state, go = blockIdx.z * sd.grad;
+    a = el_shift(a, so);
+    t = el_shift(t, so);
+    r = el_shift(r, so);
+    f_next = el_shift(f_next, so);
+    f_curr = el_shift(f_curr, so);
+    g_lam += go;
+    g_mu += go;
+    g_bx += go;
+    g_bz += go;
     // K2
     float avx = a.vx[c], avz = a.vz[c];
     avx -= d_fwd_x(t.sxx, ix, iz, nx, nz, L) * g.rdx + d_bwd_z(t.sxz, ix, iz, nx, nz, L) * g.rdz;
@@ -124,18 +154,22 @@ static __global__ void el_adj_k23(ElGeom g, ElParams p, ElState a, ElState t, El
     const float vx = sp * avx, vz = sp * avz;
     a.vx[c] = vx;
     a.vz[c] = vz;
-    r.vx[c] = g.dt * p.bx[c] * vx;
-    r.vz[c] = g.dt * p.bz[c] * vz;
+    r.vx[c] = g.dt * bx_[c] * vx;
+    r.vz[c] = g.dt * bz_[c] * vz;
 }
 
 // K4 of step n, followed (then_k1) by K1 of step n-1 on the same cell: K1 reads
 // only this cell's adjoint stresses, which K4 has just produced, so the two fuse
 // into one pass (the receiver residual added between them touches vz only).
-static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r, ElState t,
-                                 int then_k1)
+static __global__ void el_adj_k4(ElGeom g, ElParams p, ElStrides sd, ElState a, ElState r,
+                                 ElState t, int then_k1)
 {
     EL_CELL
     const int nx = g.nx, nz = g.nz;
+    const size_t so = blockIdx.z * sd.state;
+    a = el_shift(a, so);
+    r = el_shift(r, so);
+    t = el_shift(t, so);
     float sxx = a.sxx[c], szz = a.szz[c], sxz = a.sxz[c];
     sxx -= d_bwd_x(r.vx, ix, iz, nx, nz, L) * g.rdx;
     szz -= d_bwd_z(r.vz, ix, iz, nx, nz, L) * g.rdz;
@@ -145,7 +179,7 @@ static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r, ElS
         sxx = qxx;
         szz = qzz;
         sxz = qxz;
-        const float l = p.lam[c], m = p.mu[c];
+        const float l = lam_[c], m = mu_[c];
         t.sxx[c] = g.dt * ((l + 2.0f * m) * qxx + l * qzz);
         t.szz[c] = g.dt * (l * qxx + (l + 2.0f * m) * qzz);
         t.sxz[c] = g.dt * m * qxz;
@@ -158,11 +192,16 @@ static __global__ void el_adj_k4(ElGeom g, ElParams p, ElState a, ElState r, ElS
 // Vertical-strain receivers of u_{n+1} (the source term is added by the step's
 // velocity phase, elastic_kernels.cuh).
 
-static __global__ void el_sample_kernel(ElGeom g, const float* vz, const int* rec_ix, int n_rec,
-                                        int rec_iz, float* out)
+// One row of traces per shot (blockIdx.y): vz of shot s at + s * state_stride, its
+// row at out + s * out_stride.
+static __global__ void el_sample_kernel(ElGeom g, const float* vz, size_t state_stride,
+                                        const int* rec_ix, int n_rec, int rec_iz, float* out,
+                                        size_t out_stride)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_rec) return;
+    vz += blockIdx.y * state_stride;
+    out += blockIdx.y * out_stride;
     out[k] = d_bwd_z(vz, rec_ix[k], rec_iz, g.nx, g.nz, g.ldx) * g.rdz;
 }
 
@@ -171,11 +210,14 @@ static __global__ void el_sample_kernel(ElGeom g, const float* vz, const int* re
 // One thread per column; receivers sharing a column (CSR rec_ptr / rec_list, in
 // index order) add into its cells one after another, so every cell receives its
 // contributions in receiver order.
-static __global__ void el_adj_receivers(ElGeom g, float* adj_vz, const int* rec_ptr,
-                                        const int* rec_list, int rec_iz, const float* resid)
+static __global__ void el_adj_receivers(ElGeom g, float* adj_vz, size_t state_stride,
+                                        const int* rec_ptr, const int* rec_list, int rec_iz,
+                                        const float* resid, size_t resid_stride)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     if (ix >= g.nx) return;
+    adj_vz += blockIdx.y * state_stride;  // shot blockIdx.y
+    resid += blockIdx.y * resid_stride;
     const int k0 = rec_ptr[ix], k1 = rec_ptr[ix + 1];
     if (k0 == k1) return;
     const float c1 = 9.0f / 8.0f, c2 = -1.0f / 24.0f;

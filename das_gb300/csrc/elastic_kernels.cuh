@@ -41,15 +41,20 @@ struct ElGeom {
     const float* sponge;  // pitched, or null
 };
 
-// One launch of a phase: source and destination states (5 planes each, plane
-// stride `plane` floats), parameters (pitched planes), optional source term.
+// One launch of a phase over n_shots shots (blockIdx.z): source and destination
+// states (5 planes each, plane stride `plane` floats; shot s at + s * 5 * plane),
+// parameters (pitched planes; shot s at + s * pstride), optional source term.
 struct ElStep {
     const float* src;
     float* dst;
     size_t plane;
     const float *lam, *mu, *bx, *bz;
-    int inj_ix, inj_iz;       // velocity phase: vz[inj] += w[0] * dt first (inj_w non-null)
-    const float* inj_w;
+    size_t pstride;
+    // velocity phase: vz[src_pos[2s+1], src_pos[2s]] += wav[s*nt + n] * dt first
+    // (src_pos null: no source term)
+    const int* src_pos;
+    const float* wav;
+    int nt, n;
     unsigned* err;
 };
 
@@ -155,15 +160,15 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* bzz = smem + 2 * T::BOX;  // szz box
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 3 * T::BOX);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ;
+    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
         prefetch_tensormap(&maps.src);
         mbar_init(bar, 1);
         fence_mbar_init();
         mbar_expect_tx(bar, 3u * T::BOX * 4u);
-        tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, EL_SXX, bar);
-        tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, EL_SXZ, bar);
-        tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, EL_SZZ, bar);
+        tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXX, bar);
+        tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXZ, bar);
+        tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SZZ, bar);
     }
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
@@ -176,11 +181,20 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;
     const bool in_place = s.src == s.dst;
-    const float* vx_s = s.src + (size_t)EL_VX * s.plane;
-    const float* vz_s = s.src + (size_t)EL_VZ * s.plane;
-    float* vx_d = s.dst + (size_t)EL_VX * s.plane;
-    float* vz_d = s.dst + (size_t)EL_VZ * s.plane;
-    const float inj = s.inj_w ? fmul(__ldg(s.inj_w), g.dt) : 0.0f;
+    const size_t so = (size_t)sh * 5 * s.plane, po = (size_t)sh * s.pstride;
+    const float* vx_s = s.src + so + (size_t)EL_VX * s.plane;
+    const float* vz_s = s.src + so + (size_t)EL_VZ * s.plane;
+    float* vx_d = s.dst + so + (size_t)EL_VX * s.plane;
+    float* vz_d = s.dst + so + (size_t)EL_VZ * s.plane;
+    const float* bxp = s.bx + po;
+    const float* bzp = s.bz + po;
+    int inj_ix = -1, inj_iz = -1;
+    float inj = 0.0f;
+    if (s.src_pos) {
+        inj_ix = __ldg(s.src_pos + 2 * sh);
+        inj_iz = __ldg(s.src_pos + 2 * sh + 1);
+        inj = fmul(__ldg(s.wav + (size_t)sh * s.nt + s.n), g.dt);
+    }
     const int zr0 = z0 + warp * RPW;
     const int sr = zr0 - (z0 - 2);  // box row of global row zr0
     // z windows: sxz rows z-2..z+1, szz rows z-1..z+2
@@ -200,15 +214,15 @@ __global__ void __launch_bounds__(WARPS * 32)
             const size_t off = (size_t)iz * g.ldx + ixb;
             const float4 vx4 = __ldg(reinterpret_cast<const float4*>(vx_s + off));
             float4 vz4 = __ldg(reinterpret_cast<const float4*>(vz_s + off));
-            const float4 bx4 = __ldg(reinterpret_cast<const float4*>(s.bx + off));
-            const float4 bz4 = __ldg(reinterpret_cast<const float4*>(s.bz + off));
+            const float4 bx4 = __ldg(reinterpret_cast<const float4*>(bxp + off));
+            const float4 bz4 = __ldg(reinterpret_cast<const float4*>(bzp + off));
             const float4 sp4 = g.sponge ? __ldg(reinterpret_cast<const float4*>(g.sponge + off))
                                         : make_float4(1.f, 1.f, 1.f, 1.f);
             float ux[4], uz[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float vz_in = el_c(vz4, j);
-                if (s.inj_w && iz == s.inj_iz && ixb + j == s.inj_ix) vz_in = fadd(vz_in, inj);
+                if (iz == inj_iz && ixb + j == inj_ix) vz_in = fadd(vz_in, inj);
                 const float a = fmul(el_dfwd(exx[j + 1], exx[j + 2], exx[j + 3], exx[j + 4]), g.rdx);
                 const float b = fmul(el_dbwd(el_c(xz0, j), el_c(xz1, j), el_c(xz2, j), el_c(xz3, j)),
                                      g.rdz);
@@ -247,14 +261,14 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* bvz = smem + T::BOX;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::BOX);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ;
+    const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
         prefetch_tensormap(&maps.dst);
         mbar_init(bar, 1);
         fence_mbar_init();
         mbar_expect_tx(bar, 2u * T::BOX * 4u);
-        tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, EL_VX, bar);
-        tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, EL_VZ, bar);
+        tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
+        tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
     }
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
@@ -265,12 +279,15 @@ __global__ void __launch_bounds__(WARPS * 32)
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;  // see the velocity phase
     const bool in_place = s.src == s.dst;
-    const float* sxx_s = s.src + (size_t)EL_SXX * s.plane;
-    const float* szz_s = s.src + (size_t)EL_SZZ * s.plane;
-    const float* sxz_s = s.src + (size_t)EL_SXZ * s.plane;
-    float* sxx_d = s.dst + (size_t)EL_SXX * s.plane;
-    float* szz_d = s.dst + (size_t)EL_SZZ * s.plane;
-    float* sxz_d = s.dst + (size_t)EL_SXZ * s.plane;
+    const size_t so = (size_t)sh * 5 * s.plane, po = (size_t)sh * s.pstride;
+    const float* sxx_s = s.src + so + (size_t)EL_SXX * s.plane;
+    const float* szz_s = s.src + so + (size_t)EL_SZZ * s.plane;
+    const float* sxz_s = s.src + so + (size_t)EL_SXZ * s.plane;
+    float* sxx_d = s.dst + so + (size_t)EL_SXX * s.plane;
+    float* szz_d = s.dst + so + (size_t)EL_SZZ * s.plane;
+    float* sxz_d = s.dst + so + (size_t)EL_SXZ * s.plane;
+    const float* lamp = s.lam + po;
+    const float* mup = s.mu + po;
     const int zr0 = z0 + warp * RPW;
     const int sr = zr0 - (z0 - 2);
     // z windows: vx rows z-1..z+2, vz rows z-2..z+1
@@ -288,8 +305,8 @@ __global__ void __launch_bounds__(WARPS * 32)
         el_xrow(bvz, sr + r, lane, evz);
         if (iz < g.nz && col_ok) {
             const size_t off = (size_t)iz * g.ldx + ixb;
-            const float4 lam4 = __ldg(reinterpret_cast<const float4*>(s.lam + off));
-            const float4 mu4 = __ldg(reinterpret_cast<const float4*>(s.mu + off));
+            const float4 lam4 = __ldg(reinterpret_cast<const float4*>(lamp + off));
+            const float4 mu4 = __ldg(reinterpret_cast<const float4*>(mup + off));
             const float4 sxx4 = __ldg(reinterpret_cast<const float4*>(sxx_s + off));
             const float4 szz4 = __ldg(reinterpret_cast<const float4*>(szz_s + off));
             const float4 sxz4 = __ldg(reinterpret_cast<const float4*>(sxz_s + off));
@@ -370,17 +387,18 @@ __global__ void __launch_bounds__(WARPS * 32)
 
 constexpr int EL_WARPS = 4, EL_RPW = 4;
 
-// The 3D tensor map of a 5-plane state for these kernels.
+// The 3D tensor map of the 5-plane states of n_shots shots stored one after another.
 inline int make_el_state_map(CUtensorMap* m, const float* base, int nx, int nz, int ldx,
-                             size_t plane)
+                             size_t plane, int n_shots = 1)
 {
-    return make_tensor_map_3d(m, base, nx, nz, 5, ldx, plane, EL_SW,
+    return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW,
                               ElTile<EL_WARPS, EL_RPW>::TZ + 4);
 }
 
-// Velocity then stress phase of one step (src -> dst; src == dst updates in place).
+// Velocity then stress phase of one step of n_shots shots (src -> dst; src == dst
+// updates in place).
 inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, const ElStep& s,
-                                       cudaStream_t st)
+                                       cudaStream_t st, int n_shots = 1)
 {
     using T = ElTile<EL_WARPS, EL_RPW>;
     const int vbytes = 3 * T::BOX * 4 + 128, sbytes = 2 * T::BOX * 4 + 128;
@@ -394,10 +412,10 @@ inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, cons
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ);
+    dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
     elastic_velocity_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, vbytes, st>>>(maps, g, s);
     ElStep s2 = s;
-    s2.inj_w = nullptr;
+    s2.src_pos = nullptr;
     elastic_stress_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, sbytes, st>>>(maps, g, s2);
     return cudaGetLastError();
 }

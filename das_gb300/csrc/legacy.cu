@@ -219,8 +219,10 @@ int legacy_elastic(float* vx, float* vz, float* sxx, float* szz, float* sxz, con
     st.mu = d[6];
     st.bx = d[7];
     st.bz = d[8];
-    st.inj_ix = st.inj_iz = -1;
-    st.inj_w = nullptr;
+    st.pstride = 0;
+    st.src_pos = nullptr;  // no source term
+    st.wav = nullptr;
+    st.nt = st.n = 0;
     st.err = g.err;
     W2D_CUDA_TRY(launch_elastic_step(geo, maps, st, g.st));
     {

@@ -62,41 +62,61 @@ def gardner_parameters(vs: torch.Tensor, vp_over_vs: float = 1.73):
 
 
 class ElasticModeling(torch.autograd.Function):
+    """Traces of one shot (parameters (nz, nx), wavelet (nt,), scalar source) or of a
+    batch of shots (parameters (S, nz, nx), wavelets (S, nt) or (nt,), source indices
+    of length S), all shots advanced together; the backward pass returns one gradient
+    per shot."""
+
     @staticmethod
     def forward(ctx, lam, mu, bx, bz, solver: ElasticSolver2D, wavelet, source_ix, source_iz,
                 receiver_ix, receiver_iz):
         ps = [t.detach().to(torch.float32).contiguous() for t in (lam, mu, bx, bz)]
+        batched = ps[0].dim() == 3
+        S = ps[0].shape[0] if batched else 1
         for t in ps:
-            if not t.is_cuda or tuple(t.shape) != (solver.nz, solver.nx):
-                raise ValueError("parameters must be CUDA tensors of shape (nz, nx)")
-        w = np.ascontiguousarray(wavelet, dtype=np.float32).reshape(-1)
+            if not t.is_cuda or tuple(t.shape[-2:]) != (solver.nz, solver.nx) or \
+                    t.dim() != ps[0].dim() or (batched and t.shape[0] != S):
+                raise ValueError("parameters must be CUDA tensors of shape (nz, nx) or "
+                                 "(S, nz, nx)")
+        w = np.ascontiguousarray(wavelet, dtype=np.float32)
+        if w.ndim == 1:
+            w = np.ascontiguousarray(np.broadcast_to(w, (S, w.shape[0])))
+        if w.shape[0] != S:
+            raise ValueError("one wavelet per shot")
+        nt = w.shape[1]
+        six = np.asarray([normalize_index(int(x), solver.nx, "source_ix")
+                          for x in np.broadcast_to(np.asarray(source_ix), (S,))], dtype=np.int32)
+        siz = np.asarray([normalize_index(int(x), solver.nz, "source_iz")
+                          for x in np.broadcast_to(np.asarray(source_iz), (S,))], dtype=np.int32)
         rix = normalize_indices(receiver_ix, solver.nx, "receiver_ix")
-        six = normalize_index(source_ix, solver.nx, "source_ix")
-        siz = normalize_index(source_iz, solver.nz, "source_iz")
         riz = normalize_index(receiver_iz, solver.nz, "receiver_iz")
-        traces = torch.empty((len(w), len(rix)), dtype=torch.float32, device=ps[0].device)
+        traces = torch.empty((S, nt, len(rix)), dtype=torch.float32, device=ps[0].device)
         torch.cuda.current_stream(ps[0].device).synchronize()
-        _lib.check(solver._lib.w2d_elastic_forward(
-            solver._h, *[t.data_ptr() for t in ps], w.ctypes.data, len(w), six, siz,
-            rix.ctypes.data, len(rix), riz, traces.data_ptr()))
+        _lib.check(solver._lib.w2d_elastic_forward_batch(
+            solver._h, S, *[t.data_ptr() for t in ps], w.ctypes.data, nt, six.ctypes.data,
+            siz.ctypes.data, rix.ctypes.data, len(rix), riz, traces.data_ptr()))
         ctx.solver = solver
         ctx.shape = tuple(ps[0].shape)
         ctx.device = ps[0].device
-        return traces
+        return traces if batched else traces[0]
 
     @staticmethod
     def backward(ctx, grad_traces):
         g = grad_traces.detach().to(torch.float32).contiguous()
         outs = [torch.empty(ctx.shape, dtype=torch.float32, device=ctx.device) for _ in range(4)]
         torch.cuda.current_stream(ctx.device).synchronize()
-        _lib.check(ctx.solver._lib.w2d_elastic_gradient(ctx.solver._h, g.data_ptr(),
-                                                        *[o.data_ptr() for o in outs]))
+        _lib.check(ctx.solver._lib.w2d_elastic_gradient_batch(ctx.solver._h, g.data_ptr(),
+                                                              *[o.data_ptr() for o in outs]))
         return (*outs, None, None, None, None, None, None)
 
 
 def elastic_traces(vs: torch.Tensor, solver: ElasticSolver2D, wavelet, source_ix, source_iz,
                    receiver_ix, receiver_iz=2):
-    """Vertical-strain traces (nt, n_rec) for a shear-velocity model; differentiable in vs."""
+    """Vertical-strain traces for a shear-velocity model; differentiable in vs.
+
+    vs (nz, nx) with one source: traces (nt, n_rec).  vs (S, nz, nx) (one model per
+    shot, possibly equal) with S sources and wavelets: traces (S, nt, n_rec), all shots
+    advanced together."""
     return ElasticModeling.apply(*gardner_parameters(vs), solver, wavelet, source_ix, source_iz,
                                  receiver_ix, receiver_iz)
 
@@ -105,12 +125,13 @@ class ElasticExecutor:
     """Runs elastic migration jobs on worker threads, each with its own CUDA stream, so
     they overlap each other and the acoustic batch on the device.  A job's shots carry
     the shear velocity in ``vel_fwd`` and observed vertical-strain traces in ``data``;
-    each shot's result is (dJ/dvs, None) for J = 0.5 * ||d(vs) - data||^2.  Shots are
-    the unit of work (a job's shots spread over the workers); a worker keeps the solver
-    of the grid it ran last and drops it when the grid changes, so device memory holds
-    at most one elastic engine per worker."""
+    each shot's result is (dJ/dvs, None) for J = 0.5 * ||d(vs) - data||^2.  A job's
+    shots run as batches (all shots of a batch advanced by the same launches), as many
+    per batch as ``budget_gb`` of device memory holds; batches spread over the workers.
+    A worker keeps the solver of the grid it ran last and drops it when the grid
+    changes."""
 
-    def __init__(self, workers: int = 3):
+    def __init__(self, workers: int = 3, budget_gb: float = 20.0):
         import queue
         import threading
         self._q = queue.Queue()
@@ -119,6 +140,7 @@ class ElasticExecutor:
         self._pending = 0
         self._jobs = {}  # job_id -> [request, results, shots left]
         self._solvers = {}
+        self.budget = int(budget_gb * (1 << 30))  # device bytes per worker for one batch
         self._threads = [threading.Thread(target=self._loop, daemon=True)
                          for _ in range(max(1, int(workers)))]
         for t in self._threads:
@@ -138,13 +160,46 @@ class ElasticExecutor:
 
     @staticmethod
     def migrate_shot(solver, shot):
-        vs = torch.tensor(np.asarray(shot.vel_fwd, np.float32), device="cuda", requires_grad=True)
-        d = elastic_traces(vs, solver, shot.wavelet, shot.source_ix, shot.source_iz,
-                           shot.receiver_ix, shot.receiver_iz)
-        obs = torch.tensor(np.asarray(shot.data, np.float32), device="cuda")
+        return ElasticExecutor.migrate_shots(solver, [shot])[0]
+
+    @staticmethod
+    def migrate_shots(solver, shots):
+        """Shots on one grid as one batch: per shot (dJ/dvs, None) for
+        J = 0.5 * ||d(vs) - data||^2."""
+        vs = torch.tensor(np.stack([np.asarray(s.vel_fwd, np.float32) for s in shots]),
+                          device="cuda", requires_grad=True)
+        d = elastic_traces(vs, solver, np.stack([np.asarray(s.wavelet, np.float32)
+                                                 for s in shots]),
+                           [s.source_ix for s in shots], [s.source_iz for s in shots],
+                           shots[0].receiver_ix, shots[0].receiver_iz)
+        obs = torch.tensor(np.stack([np.asarray(s.data, np.float32) for s in shots]),
+                           device="cuda")
         J = 0.5 * torch.sum((d - obs) ** 2)
         J.backward()
-        return vs.grad.detach().cpu().numpy(), None
+        g = vs.grad.detach().cpu().numpy()
+        return [(g[k], None) for k in range(len(shots))]
+
+    def _batches(self, shots):
+        """Consecutive runs of shots that share a grid, receivers and length, each at
+        most as large as the per-worker memory budget allows."""
+        out, cur = [], []
+        for s in shots:
+            same = cur and self._key(s) == self._key(cur[0]) and \
+                len(s.wavelet) == len(cur[0].wavelet) and \
+                np.array_equal(np.asarray(s.receiver_ix), np.asarray(cur[0].receiver_ix)) and \
+                s.receiver_iz == cur[0].receiver_iz
+            if cur and (not same or len(cur) >= self._cap(cur[0])):
+                out.append(cur)
+                cur = []
+            cur.append(s)
+        if cur:
+            out.append(cur)
+        return out
+
+    def _cap(self, shot):
+        per = int(_lib.load().w2d_elastic_shot_bytes(shot.nx, shot.nz, len(shot.wavelet),
+                                                     len(np.asarray(shot.receiver_ix))))
+        return max(1, min(64, self.budget // max(per, 1)))
 
     def _loop(self):
         import time
@@ -156,21 +211,23 @@ class ElasticExecutor:
                 if solver is not None:
                     solver.close()
                 return
-            jid, k = item
+            jid, ks = item
             with self._lock:
                 req = self._jobs[jid][0]
-            shot = req.shots[k]
-            if self._key(shot) != key:
+            shots = [req.shots[k] for k in ks]
+            if self._key(shots[0]) != key:
                 if solver is not None:
                     solver.close()
-                key = self._key(shot)
-                solver = ElasticSolver2D(shot.nx, shot.nz, shot.dx, shot.dz, shot.dt,
-                                         shot.n_sponge, shot.sponge_alpha, shot.free_surface_top)
-            res = self.migrate_shot(solver, shot)
+                key = self._key(shots[0])
+                s0 = shots[0]
+                solver = ElasticSolver2D(s0.nx, s0.nz, s0.dx, s0.dz, s0.dt, s0.n_sponge,
+                                         s0.sponge_alpha, s0.free_surface_top)
+            res = self.migrate_shots(solver, shots)
             with self._lock:
                 entry = self._jobs[jid]
-                entry[1][k] = res
-                entry[2] -= 1
+                for k, r in zip(ks, res):
+                    entry[1][k] = r
+                entry[2] -= len(ks)
                 if entry[2] == 0:
                     self._done.append((jid, entry[1], time.perf_counter()))
                     del self._jobs[jid]
@@ -180,8 +237,10 @@ class ElasticExecutor:
         with self._lock:
             self._pending += 1
             self._jobs[req.job_id] = [req, [None] * len(req.shots), len(req.shots)]
-        for k in range(len(req.shots)):
-            self._q.put((req.job_id, k))
+        k0 = 0
+        for batch in self._batches(req.shots):
+            self._q.put((req.job_id, list(range(k0, k0 + len(batch)))))
+            k0 += len(batch)
 
     def pending(self) -> int:
         with self._lock:

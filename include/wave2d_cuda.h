@@ -195,6 +195,19 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
 int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
                          float* g_bx, float* g_bz);
 float w2d_elastic_last_ms(w2d_elastic* e);
+/* The same for a batch of n_shots shots on this grid, advanced together (every
+ * launch covers all shots): lam, mu, bx, bz DEVICE n_shots x (nz, nx) contiguous
+ * (each shot its own model), wavelets HOST (n_shots, nt), src_ix / src_iz HOST
+ * n_shots each, receivers shared, traces_dev DEVICE (n_shots, nt, n_rec); the
+ * gradient of the last batch returns one gradient per shot (n_shots x (nz, nx)). */
+int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, const float* mu,
+                              const float* bx, const float* bz, const float* wavelets, int nt,
+                              const int* src_ix, const int* src_iz, const int* rec_ix, int n_rec,
+                              int rec_iz, float* traces_dev);
+int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
+                               float* g_bx, float* g_bz);
+/* Device bytes one shot of a batch holds (checkpoints, one recomputed segment, fields). */
+unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 
 /* ---- Part 3: batched / continuously fed migration (no reference counterpart:
  * the reference migrates shots one after another, rtm_engine.py:125-143) ----- */
