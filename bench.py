@@ -32,6 +32,7 @@ import os
 import re
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -111,7 +112,9 @@ class Clocks:
     def __init__(self, gpu_id: str, rank: int):
         self.proc = None
         self.gpu = gpu_id
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_rank{rank}.csv")
+        # the samples go to BENCH_CLOCKS_DIR when set (to keep them), else a temporary folder
+        out_dir = os.environ.get("BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"das_gb300_clocks_rank{rank}.csv")
 
     def start(self):
         try:
@@ -218,6 +221,42 @@ def run_reference(args, dist):
                             "sample": sample},
            "e2e": {"value": gpts, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def accuracy_statement():
+    """Parity and float64 error of the GPU migration on a reduced grid of the same model
+    family (120 x 480, dx 10 m, dt 1 ms, nt 500, 480 receivers): the image and
+    illumination against the oracle's float32 restatement (the reference's arithmetic,
+    expected bit-identical) and against its float64 run of the same stencil.  The oracle
+    runs on the host (test infrastructure; not part of the timed work)."""
+    from oracle import oracle as o
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D
+    from das_gb300.synthetic import _layered_faulted
+    from scipy.ndimage import gaussian_filter
+    nz, nx, d, dt, nt = 120, 480, 10.0, 1e-3, 500
+    zmax = (nz - 1) * d
+    vt = _layered_faulted(nz, nx, d, d, 0.45 * zmax, 0.12 * zmax, 0.0,
+                          [(0.5 * (nx - 1) * d, 60.0, 0.05 * zmax)], v1=3000.0).astype(np.float32)
+    vm = gaussian_filter(vt.astype(np.float64), 5.0).astype(np.float32)
+    w, _ = o.ricker_wavelet(6.0, dt, nt * dt)
+    grid = o.Grid(nx, nz, d, d, dt, 40, 0.0015, True)
+    rix = np.arange(nx)
+    data, _ = o.forward_propagate_acoustic(grid, vt, w, nx // 2, 2, rix, 2)
+    img32, ill32 = o.migrate_shot(grid, vm, vm, w, nx // 2, 2, data, rix, 2, 2)
+    img64, ill64 = o.migrate_shot(grid, vm, vm, w, nx // 2, 2, data, rix, 2, 2, precision="f64")
+    s = WaveSolver2D(nx, nz, d, d, dt, 40, 0.0015, True)
+    img, ill = TSWRTMEngine(s, "all").migrate_shot(FloodModels(vt, vm, vm, 0, 0), w, nx // 2, 2,
+                                                   data, rix, 2, 2)
+    s.close()
+    return {"case": "120x480, nt 500, one shot (same model family)",
+            "image_vs_reference_f32_rel_l2": o.rel_l2(img, img32),
+            "image_max_abs_diff_vs_reference_f32": float(np.max(np.abs(img - img32))),
+            "illum_vs_reference_f32_rel_l2": o.rel_l2(ill, ill32),
+            "image_vs_fp64_rel_l2": o.rel_l2(img, img64),
+            "illum_vs_fp64_rel_l2": o.rel_l2(ill, ill64),
+            "tolerance_image_rel_l2": 1e-4}
 
 
 def run_ours(args, dist):
@@ -332,6 +371,8 @@ def run_ours(args, dist):
                "sample": f"migrate_shot on the 1000x4000 grid truncated to nt={args.cpu_nt} "
                          f"(forward+backward, interval 2, 4000 receivers), {el:.1f} s"}
 
+    acc = accuracy_statement() if dist.rank == 0 and args.accuracy else None
+
     if dist.rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": K,
                "warmup": W, "ms_per_step": dev_s * 1e3 / K, "higher_is_better": True,
@@ -354,7 +395,7 @@ def run_ours(args, dist):
                        "d2h_bytes_per_step": int(d2h), "steps": ke,
                        "api": "TSWRTMEngine.migrate_shot (pinned host arrays)"},
                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-               "wall_s_timed_region": wall}
+               "wall_s_timed_region": wall, "accuracy": acc}
         print(json.dumps(out), flush=True)
 
 
@@ -704,6 +745,7 @@ def main():
     ap.add_argument("--tile", default="")
     ap.add_argument("--cpu-nt", type=int, default=1500)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--accuracy", type=int, default=1)
     ap.add_argument("--distinct-gathers", type=int, default=2)
     args = ap.parse_args()
     os.environ.setdefault("OMP_NUM_THREADS", str(len(os.sched_getaffinity(0))))

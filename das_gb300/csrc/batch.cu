@@ -71,6 +71,10 @@ struct w2d_batch {
     int form = 1;    // 1: one launch per phase step over all shots (grid form); 0: queue form
     int t_all = 0;   // tiles of the active shots (grid form launch size)
     cudaGraphExec_t gexec = nullptr;
+    // grid form: the replay's launches as a graph, re-captured when the active set
+    // (grid size, shot count) or the configuration changes
+    cudaGraphExec_t gexec_grid = nullptr;
+    long long grid_key = -1;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<cudaEvent_t> ready;  // per slot: admission work finished
     std::vector<int> joining;        // admitted shots that join at the next launch
@@ -142,7 +146,7 @@ cudaError_t set_attr_and_occ(int* grid)
 }
 
 template <int W, int R>
-cudaError_t launch_batch_step(const BatchStepArgs& a, int grid, cudaStream_t st, int pdl)
+cudaError_t batch_step_attr()
 {
     using T = AcTile<W, R, SPONGE_LUT>;
     static bool attr_set = false;  // one attribute call per instantiation
@@ -153,6 +157,21 @@ cudaError_t launch_batch_step(const BatchStepArgs& a, int grid, cudaStream_t st,
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    return cudaSuccess;
+}
+
+cudaError_t batch_step_attr_cfg(const w2d_batch* b)
+{
+    if (b->warps == 4 && b->rpw == 4) return batch_step_attr<4, 4>();
+    if (b->warps == 4 && b->rpw == 8) return batch_step_attr<4, 8>();
+    if (b->warps == 8 && b->rpw == 8) return batch_step_attr<8, 8>();
+    return batch_step_attr<8, 4>();
+}
+
+template <int W, int R>
+cudaError_t launch_batch_step(const BatchStepArgs& a, int grid, cudaStream_t st, int pdl)
+{
+    using T = AcTile<W, R, SPONGE_LUT>;
     return launch_ex(acoustic_batch_step_kernel<W, R>, dim3(grid), dim3(W * 32), T::SMEM_BYTES,
                      st, pdl, a);
 }
@@ -188,6 +207,60 @@ void launch_cfg(w2d_batch* b, const BatchArgs& a)
     else if (b->warps == 4 && b->rpw == 8) launch_batch<4, 8>(a, b->grid, b->st);
     else if (b->warps == 8 && b->rpw == 8) launch_batch<8, 8>(a, b->grid, b->st);
     else launch_batch<8, 4>(a, b->grid, b->st);
+}
+
+// Capture the grid form's replay: `steps` launches (the first waits for the stream
+// normally, the others are programmatic dependents of the one before) and the
+// progress advance.  An existing executable graph is updated in place when the
+// topology allows, else replaced.
+int capture_grid_replay(w2d_batch* b, int steps)
+{
+    BatchStepArgs a;
+    a.shots = b->d_shots;
+    a.maps = b->d_maps;
+    a.active = b->d_active;
+    a.tile_prefix = b->d_prefix;
+    a.n_active = (int)b->active.size();
+    a.max_shots = b->max_shots;
+    a.err = b->d_err;
+    cudaGraph_t g = nullptr;
+    W2D_CUDA_TRY(batch_step_attr_cfg(b));  // outside the capture
+    W2D_CUDA_TRY(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaSuccess;
+    for (int j = 0; j < steps && ce == cudaSuccess; ++j) {
+        a.j = j;
+        ce = launch_step_cfg(b, a, j > 0 ? 1 : 0);
+    }
+    if (ce == cudaSuccess) {
+        batch_advance_kernel<<<(b->max_shots + 127) / 128, 128, 0, b->st>>>(b->d_shots, b->d_active,
+                                                                             b->d_nact, steps);
+        ce = cudaGetLastError();
+    }
+    const cudaError_t ee = cudaStreamEndCapture(b->st, &g);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        set_error(std::string("replay capture failed: ") +
+                  cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+        return W2D_ECUDA;
+    }
+    if (b->gexec_grid) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(b->gexec_grid, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(b->gexec_grid);
+            b->gexec_grid = nullptr;
+        }
+    }
+    if (!b->gexec_grid) {
+        ce = cudaGraphInstantiate(&b->gexec_grid, g, 0);
+        if (ce != cudaSuccess) {
+            cudaGraphDestroy(g);
+            set_error(std::string("replay instantiation failed: ") + cudaGetErrorString(ce));
+            return W2D_ECUDA;
+        }
+    }
+    cudaGraphDestroy(g);
+    return W2D_OK;
 }
 
 int build_graph(w2d_batch* b)
@@ -290,6 +363,7 @@ void w2d_batch_destroy(w2d_batch* b)
     if (!b) return;
     if (b->st) cudaStreamSynchronize(b->st);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->gexec_grid) cudaGraphExecDestroy(b->gexec_grid);
     for (void* p : {(void*)b->arena, (void*)b->d_shots, (void*)b->d_maps, (void*)b->d_active,
                     (void*)b->d_prefix, (void*)b->d_nact, (void*)b->d_head, (void*)b->d_err})
         if (p) cudaFree(p);
@@ -324,6 +398,11 @@ int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_p
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
+    if (b->gexec_grid) {
+        cudaGraphExecDestroy(b->gexec_grid);
+        b->gexec_grid = nullptr;
+    }
+    b->grid_key = -1;
     return W2D_OK;
 }
 
@@ -609,24 +688,17 @@ int w2d_batch_launch(w2d_batch* b)
     }
     if (b->form == 1) {
         // grid form: S * chunks launches, one phase step of every active shot each,
-        // then one advance of the shots' progress
+        // then one advance of the shots' progress, replayed as one captured graph
         const int steps = b->S * b->chunks;
-        BatchStepArgs a;
-        a.shots = b->d_shots;
-        a.maps = b->d_maps;
-        a.active = b->d_active;
-        a.tile_prefix = b->d_prefix;
-        a.n_active = (int)b->active.size();
-        a.max_shots = b->max_shots;
-        a.err = b->d_err;
-        W2D_CUDA_TRY(cudaEventRecord(b->e0, b->st));
-        for (int j = 0; j < steps; ++j) {
-            a.j = j;
-            W2D_CUDA_TRY(launch_step_cfg(b, a, j > 0 ? 1 : 0));
+        const long long key =
+            (((long long)b->t_all * 65536 + (long long)b->active.size()) * 4096 + steps) * 256 +
+            b->warps * 16 + b->rpw;
+        if (b->grid_key != key || !b->gexec_grid) {
+            if ((rc = capture_grid_replay(b, steps))) return rc;
+            b->grid_key = key;
         }
-        batch_advance_kernel<<<(b->max_shots + 127) / 128, 128, 0, b->st>>>(b->d_shots, b->d_active,
-                                                                             b->d_nact, steps);
-        W2D_CUDA_TRY(cudaGetLastError());
+        W2D_CUDA_TRY(cudaEventRecord(b->e0, b->st));
+        W2D_CUDA_TRY(cudaGraphLaunch(b->gexec_grid, b->st));
         W2D_CUDA_TRY(cudaEventRecord(b->e1, b->st));
         b->last_launches = steps + 1;
         b->in_flight = true;
