@@ -49,26 +49,28 @@ def test_standing_wave_is_exact_for_the_discrete_scheme(cuda_lib, ppw):
     w_num = np.arccos(c) / dt
     err = w_num / (v * k) - 1.0
     print(f"{ppw} points per wavelength: phase velocity error {err:+.2e}")
-    if ppw >= 10:
-        assert abs(err) < 2e-3
-    else:
-        assert abs(err) < 6e-2
+    # the known behaviour of the scheme: negligible at 10 or more points per
+    # wavelength, a few percent at 3-5
+    assert abs(err) < {40.0: 1e-4, 10.0: 1e-3, 5.0: 2e-2, 3.0: 1e-1}[ppw]
 
 
 def test_homogeneous_travel_time():
-    """Two receivers 100 and 300 cells from a buried source in a 2000 m/s medium:
-    the arrival lag between them is 200 dx / v within two samples (no free surface,
-    receivers far from the sponge; the 2D Green's function's tail changes the pulse
-    shape slightly with distance)."""
+    """Two receivers 100 and 300 cells from a buried source in a 2000 m/s medium: the
+    lag between their direct arrivals is 200 dx / v within two samples.  The grid keeps
+    the sponge's reflections out of the windows (the Cerjan sponge of the scheme
+    reflects low frequencies noticeably), and no free surface."""
     from das_gb300.wave_solver import WaveSolver2D, ricker_wavelet
-    nz, nx, dx, dt, v = 240, 900, 5.0, 5e-4, 2000.0
+    nz, nx, dx, dt, v = 400, 900, 5.0, 5e-4, 2000.0
     s = WaveSolver2D(nx, nz, dx, dx, dt, n_sponge=40, free_surface_top=False)
     w, _ = ricker_wavelet(15.0, dt, 1.0)
-    src = (120, 150)  # (iz, ix)
+    src = (200, 150)  # (iz, ix)
     rix = np.array([src[1] + 100, src[1] + 300])
     rec, _ = s.forward_propagate_acoustic(np.full((nz, nx), v, np.float32), w, src[1], src[0], rix,
                                           src[0])
-    a, b = rec[:, 0].astype(np.float64), rec[:, 1].astype(np.float64)
+    # direct arrivals: near at 0.25 s + the wavelet delay, far at 0.75 s + it; the first
+    # sponge reflection reaches the near receiver after 0.8 s and the far one after 1.1 s
+    a = rec[: int(0.6 / dt), 0].astype(np.float64)
+    b = rec[:, 1].astype(np.float64)
     cc = np.correlate(b, a, mode="full")
     lag = (np.argmax(cc) - (len(a) - 1)) * dt
     want = 200 * dx / v
