@@ -473,6 +473,14 @@ def run_batched(args, dist):
                           "gpts_per_s": plain_pts / plain_s / 1e9},
            "speedup_vs_plain_loop_gpts": (pts / wall) / (plain_pts / plain_s),
            "autotune": tune_table}
+    # roofline of the batch kernel at the device rate: 22 algorithmic bytes per counted
+    # point at snapshot interval 2 (16 per step; every second forward step adds 12 for the
+    # snapshot and illumination, every second backward step 12 for the imaging)
+    peak, peak_kind = measured_peaks()
+    dev = out["gpts_per_s_device"] * 1e9 * 22.0 / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": dev, "peak": peak, "unit": "GB/s",
+                       "frac": dev / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                       "kernel": "acoustic_batch_step_kernel", "bytes_per_counted_point": 22.0}
     print(json.dumps(out), flush=True)
 
 

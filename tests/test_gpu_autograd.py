@@ -81,3 +81,25 @@ def test_gradient_relates_to_rtm_image():
     c = np.corrcoef(g[m].ravel(), img[m].ravel())[0, 1]
     print(f"correlation(gradient, RTM image of the residual) = {c:.3f}")
     assert c < -0.6  # d2/dt2 ~ -omega^2: anti-correlated with the zero-lag image
+
+
+def test_gradient_of_8000_steps_on_the_large_grid():
+    """An 8000-step shot on the 1000 x 4000 grid: the forward states come back from
+    checkpoints (about sqrt(3 nt) segments of recomputation), so the gradient fits in
+    HBM; it is finite, non-zero, and its run time is reported."""
+    import time
+    from das_gb300.autograd import misfit_and_gradient
+    from das_gb300.wave_solver import WaveSolver2D, ricker_wavelet
+    nz, nx, dx, dt, nt = 1000, 4000, 2.5, 2.5e-4, 8000
+    v = (1500.0 + 1.5 * np.arange(nz)[:, None] + 0.0 * np.arange(nx)[None, :]).astype(np.float32)
+    w, _ = ricker_wavelet(6.0, dt, nt * dt)
+    rix = np.arange(0, nx, 4)
+    d_obs = np.zeros((len(w), len(rix)), np.float32)
+    s = WaveSolver2D(nx, nz, dx, dx, dt, n_sponge=30)
+    t0 = time.perf_counter()
+    J, g = misfit_and_gradient(s, v, w, nx // 2, 2, rix, 2, d_obs)
+    el = time.perf_counter() - t0
+    print(f"8000-step gradient on 1000 x 4000: {el:.2f} s, J = {J:.3e}")
+    assert np.isfinite(J) and J > 0
+    assert np.isfinite(g).all() and np.abs(g).max() > 0
+    s.close()
