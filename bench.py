@@ -550,6 +550,7 @@ def run_elastic(args, dist):
     w = (w * 1e6).astype(np.float32)
     rix = np.arange(2, nx - 2)
     solver = ElasticSolver2D(nx, nz, d, d, dt, n_sponge=40, sponge_alpha=0.0015)
+    solver.set_adjoint(args.el_adjoint)
     src = [int(s) for s in np.linspace(40, nx - 41, 64).astype(int)]
     K, W = args.steps, 1
     vt = torch.tensor(vs_true, device="cuda")
@@ -577,7 +578,8 @@ def run_elastic(args, dist):
            "unit": "Gpts/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
            "data": "synthetic", "steps": K, "warmup": W,
            "config": {"workload": f"elastic velocity-stress gradient 1024x2048, dx 2 m, nt {nt}, "
-                                  f"{len(rix)} vertical-strain receivers, 5 Hz, checkpointed"},
+                                  f"{len(rix)} vertical-strain receivers, 5 Hz, checkpointed",
+                      "adjoint": args.el_adjoint},
            "s_per_shot": sum(times) / K, "device_ms_forward": statistics.mean(fwd_ms),
            "device_ms_gradient": statistics.mean(grad_ms),
            "counted_points_per_shot": pts}
@@ -729,6 +731,7 @@ def main():
                     choices=["large", "batched", "served", "elastic", "interferometry"])
     ap.add_argument("--xc-windows", type=int, default=32)
     ap.add_argument("--el-nt", type=int, default=6000)
+    ap.add_argument("--el-adjoint", default="tiled", choices=["tiled", "cells"])
     ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
     ap.add_argument("--pdl", type=int, default=1)

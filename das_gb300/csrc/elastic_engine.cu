@@ -20,7 +20,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "elastic_adjoint_kernels.cuh"
+#include "elastic_adjoint_tma.cuh"
 #include "small_kernels.cuh"
 #include "w2d_common.cuh"
 #include "wave2d_cuda.h"
@@ -59,6 +59,9 @@ struct w2d_elastic {
     unsigned* err = nullptr;                // device error word of the step kernels
     CUtensorMap map_state;                  // 3D map over the S x 5 planes of `state`
     std::vector<CUtensorMap> seg_maps;      // one per slot of `seg`
+    int adj_form = 1;                       // 1: TMA-tiled adjoint passes, 0: per-cell kernels
+    CUtensorMap adj_map_tmp;                // the adjoint passes' maps (their own box height)
+    std::vector<CUtensorMap> adj_seg_maps;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     float last_ms = 0.f;
 
@@ -279,6 +282,11 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
     for (int i = 0; i <= e->seg_len; ++i)
         if ((rc = make_el_state_map(&e->seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S)))
             return rc;
+    if ((rc = make_el_adj_map(&e->adj_map_tmp, e->tmp, e->nx, e->nz, e->ldx, P, S))) return rc;
+    e->adj_seg_maps.resize(e->seg_len + 1);
+    for (int i = 0; i <= e->seg_len; ++i)
+        if ((rc = make_el_adj_map(&e->adj_seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S)))
+            return rc;
     const size_t hp = (size_t)e->nx * 4, dp = (size_t)e->ldx * 4, np = (size_t)e->nx * e->nz;
     const float* src[4] = {lam, mu, bx, bz};
     for (int s = 0; s < S; ++s)
@@ -383,11 +391,22 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 return rc;
         }
         for (int n = b0 - 1; n >= a0; --n) {
-            ElState f_next = e->S0(e->slot(n + 1 - a0));  // u_{n+1}
-            ElState f_curr = e->S0(e->slot(n - a0));      // u_n
-            el_adj_k23<<<grd, blk, 0, e->st>>>(g, prm, sd, a, t, r, f_next, f_curr, glam, gmu, gbx,
-                                               gbz);
-            el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, sd, a, r, t, n >= 1 ? 1 : 0);
+            if (e->adj_form == 1) {
+                ElAdjMaps m;
+                m.tmp = e->adj_map_tmp;
+                m.f_next = e->adj_seg_maps[n + 1 - a0];
+                m.f_curr = e->adj_seg_maps[n - a0];
+                W2D_CUDA_TRY(launch_el_adj_a(m, g, prm, sd, a, r, glam, gmu, gbx, gbz, e->err, S,
+                                             e->st));
+                W2D_CUDA_TRY(launch_el_adj_b(m, g, prm, sd, a, t, n >= 1 ? 1 : 0, e->err, S,
+                                             e->st));
+            } else {
+                ElState f_next = e->S0(e->slot(n + 1 - a0));  // u_{n+1}
+                ElState f_curr = e->S0(e->slot(n - a0));      // u_n
+                el_adj_k23<<<grd, blk, 0, e->st>>>(g, prm, sd, a, t, r, f_next, f_curr, glam, gmu,
+                                                   gbx, gbz);
+                el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, sd, a, r, t, n >= 1 ? 1 : 0);
+            }
             if (n >= 1)
                 el_adj_receivers<<<rgrid, 128, 0, e->st>>>(g, a.vz, SS, e->rec_ptr, e->rec_list,
                                                            e->rec_iz,
@@ -419,6 +438,13 @@ int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, f
 {
     W2D_CHECK_ARG(e && e->S == 1, "the last forward call was a batch: use the batch gradient");
     return w2d_elastic_gradient_batch(e, resid_dev, g_lam, g_mu, g_bx, g_bz);
+}
+
+int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
+{
+    W2D_CHECK_ARG(e && (form == 0 || form == 1), "form must be 0 (per-cell) or 1 (tiled)");
+    e->adj_form = form;
+    return W2D_OK;
 }
 
 float w2d_elastic_last_ms(w2d_elastic* e) { return e ? e->last_ms : 0.f; }

@@ -49,6 +49,14 @@ class ElasticSolver2D:
     def last_ms(self) -> float:
         return float(self._lib.w2d_elastic_last_ms(self._h))
 
+    def set_adjoint(self, form: str = "tiled"):
+        """How the adjoint passes run: "tiled" (TMA-tiled passes, the default) or
+        "cells" (one thread per cell); both are exact adjoints of the step and agree
+        to float32 rounding."""
+        if form not in ("tiled", "cells"):
+            raise ValueError("form must be 'tiled' or 'cells'")
+        _lib.check(self._lib.w2d_elastic_set_adjoint(self._h, 1 if form == "tiled" else 0))
+
 
 def gardner_parameters(vs: torch.Tensor, vp_over_vs: float = 1.73):
     """(lambda, mu, buo_x, buo_z) from the shear velocity: vp = 1.73 vs, Gardner's

@@ -206,6 +206,9 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
                               int rec_iz, float* traces_dev);
 int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
                                float* g_bx, float* g_bz);
+/* How the adjoint passes run: 1 (default) TMA-tiled passes, 0 per-cell kernels.
+ * The two agree to float32 rounding (contraction differs); both are exact adjoints. */
+int w2d_elastic_set_adjoint(w2d_elastic* e, int form);
 /* Device bytes one shot of a batch holds (checkpoints, one recomputed segment, fields). */
 unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 

@@ -93,7 +93,7 @@ def test_gradient_of_8000_steps_on_the_large_grid():
     nz, nx, dx, dt, nt = 1000, 4000, 2.5, 2.5e-4, 8000
     v = (1500.0 + 1.5 * np.arange(nz)[:, None] + 0.0 * np.arange(nx)[None, :]).astype(np.float32)
     w, _ = ricker_wavelet(6.0, dt, nt * dt)
-    rix = np.arange(0, nx, 4)
+    rix = np.arange(2, nx - 2, 4)
     d_obs = np.zeros((len(w), len(rix)), np.float32)
     s = WaveSolver2D(nx, nz, dx, dx, dt, n_sponge=30)
     t0 = time.perf_counter()
