@@ -57,6 +57,8 @@ def _load(name: str = "liboracle.so") -> ctypes.CDLL:
     lib.oracle_correlate_f64.argtypes = [f32p] * 3 + [i, i, d]
     lib.oracle_cerjan_sponge.argtypes = [f32p, i, i, i, f, i]
     lib.oracle_num_threads.restype = ctypes.c_int
+    lib.oracle_set_num_threads.argtypes = [i]
+    lib.oracle_set_num_threads.restype = None
     for fn in ("oracle_acoustic_step_f32", "oracle_acoustic_step_f64", "oracle_elastic_step_f32",
                "oracle_elastic_step_f64", "oracle_correlate_f32", "oracle_correlate_f64",
                "oracle_cerjan_sponge"):
@@ -112,6 +114,13 @@ def backend() -> str:
 
 def num_threads(native: bool = False) -> int:
     return int(lib(native).oracle_num_threads())
+
+
+def set_num_threads(n: int) -> None:
+    """Threads of the later parallel regions (the port, the native build and the
+    reference library share the process's OpenMP runtime)."""
+    lib(False).oracle_set_num_threads(int(n))
+    lib(True).oracle_set_num_threads(int(n))
 
 
 def _ptr(a: Optional[np.ndarray]):

@@ -322,3 +322,14 @@ int oracle_num_threads(void)
     return 1;
 #endif
 }
+
+/* Thread count of later parallel regions of the calling thread (the OpenMP runtime is
+ * one per process, so this also sets it for the reference library loaded beside). */
+void oracle_set_num_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
