@@ -739,14 +739,101 @@ def run_interferometry(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def run_small(args, dist):
+    """Small plain RTM (150 x 400, dx 10 m, nt 2000, 20 shots x 400 receivers, interval 2):
+    the whole TSWRTMEngine.migrate_multiple_shots call (20 shots, stack, post-stack) on
+    the GPU, the same 20 shots as one BatchEngine batch (every launch advances all shots;
+    host stack in shot order, bit-identical to the serial stack), and the reference's
+    CPU path (oracle port of wave2d.c + its Python loops) over the same 20 shots on all
+    host cores.  Observed gathers: forward modelling in the true model on the GPU."""
+    from das_gb300.batch import BatchEngine, ShotJob
+    from das_gb300.rtm_engine import TSWRTMEngine, post_stack
+    from das_gb300.synthetic import plain_small
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D
+    sv = plain_small(seed=0)
+    n = len(sv.src_ix)
+    solver = WaveSolver2D(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, n_sponge=sv.n_sponge,
+                          sponge_alpha=sv.sponge_alpha)
+    gathers = [solver.forward_propagate_acoustic(sv.vel_true, sv.wavelet, int(s), sv.src_iz,
+                                                 sv.rec_ix, sv.rec_iz)[0] for s in sv.src_ix]
+    fm = FloodModels(sv.vel_true, sv.vel_mig, sv.vel_mig, 0, 0)
+    eng = TSWRTMEngine(solver)
+    waves = [sv.wavelet] * n
+    siz = [sv.src_iz] * n
+
+    def serial():
+        return eng.migrate_multiple_shots(fm, waves, list(sv.src_ix), siz, gathers, sv.rec_ix,
+                                          sv.rec_iz, 2)
+
+    for _ in range(args.warmup):
+        serial()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = serial()
+    serial_s = (time.perf_counter() - t0) / args.steps
+    jobs = [ShotJob(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.vel_mig, sv.vel_mig, sv.wavelet,
+                    gathers[k], sv.rec_ix, int(sv.src_ix[k]), sv.src_iz, sv.rec_iz, 2,
+                    sv.n_sponge, sv.sponge_alpha) for k in range(n)]
+    be = BatchEngine(arena_bytes=4 << 30, max_shots=n, tile=(4, 4))
+
+    def batched():
+        out, st = be.run(jobs)
+        stacked = np.zeros((sv.nz, sv.nx), np.float32)
+        illum = np.zeros((sv.nz, sv.nx), np.float32)
+        for img, ill in out:
+            stacked += img
+            illum += ill
+        return post_stack(solver, stacked, illum), st
+
+    for _ in range(args.warmup):
+        batched()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bres, bst = batched()
+    batch_s = (time.perf_counter() - t0) / args.steps
+    same = bool(np.array_equal(bres.raw_image, res.raw_image))
+    pts = n * sv.counted_points_per_shot()
+    cpu = None
+    if args.small_cpu_shots > 0:
+        threads = len(os.sched_getaffinity(0))
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        from oracle import oracle as o
+        kind = "reference" if o.reference_available() else "port"
+        o.set_backend("reference" if kind == "reference" else "native")
+        o.set_num_threads(threads)
+        g = o.Grid(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
+        k = min(n, args.small_cpu_shots)
+        t0 = time.perf_counter()
+        o.migrate_multiple_shots(g, sv.vel_mig, sv.vel_mig, waves[:k], list(sv.src_ix[:k]),
+                                 siz[:k], gathers[:k], sv.rec_ix, sv.rec_iz, 2, native=True)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": k * sv.counted_points_per_shot() / cpu_s / 1e9, "unit": UNIT,
+               "cores": threads, "kind": kind,
+               "sample": f"migrate_multiple_shots over {k} of the {n} shots, {cpu_s:.1f} s"}
+    out = {"metric": METRIC, "value": pts / batch_s / 1e9, "unit": UNIT, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": sv.name, "nz": sv.nz, "nx": sv.nx, "nt": sv.nt, "shots": n,
+                      "interval": 2},
+           "s_per_survey_batched": batch_s, "s_per_survey_serial": serial_s,
+           "gpts_per_s_serial": pts / serial_s / 1e9, "shots_per_s_batched": n / batch_s,
+           "shots_per_s_serial": n / serial_s, "batched_device_ms": bst["device_ms"],
+           "batched_stack_equals_serial": same, "cpu_baseline": cpu}
+    be.close()
+    solver.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--workload", default="large",
-                    choices=["large", "batched", "served", "elastic", "interferometry"])
+                    choices=["large", "small", "batched", "served", "elastic", "interferometry"])
     ap.add_argument("--xc-windows", type=int, default=32)
     ap.add_argument("--el-nt", type=int, default=6000)
     ap.add_argument("--el-adjoint", default="tiled", choices=["tiled", "cells"])
+    ap.add_argument("--small-cpu-shots", type=int, default=20)
     ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
     ap.add_argument("--pdl", type=int, default=1)
@@ -798,6 +885,8 @@ def main():
             run_elastic(args, dist)
         elif args.workload == "interferometry":
             run_interferometry(args, dist)
+        elif args.workload == "small":
+            run_small(args, dist)
         else:
             run_ours(args, dist)
     finally:
