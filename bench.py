@@ -566,6 +566,8 @@ def run_elastic(args, dist):
     rix = np.arange(2, nx - 2)
     solver = ElasticSolver2D(nx, nz, d, d, dt, n_sponge=40, sponge_alpha=0.0015)
     solver.set_adjoint(args.el_adjoint)
+    el_step, el_adj = ([int(v) for v in t.split(",")] for t in args.el_tiles.split(":"))
+    solver.set_tiles(el_step, el_adj)
     src = [int(s) for s in np.linspace(40, nx - 41, 64).astype(int)]
     K, W = args.steps, 1
     vt = torch.tensor(vs_true, device="cuda")
@@ -594,7 +596,7 @@ def run_elastic(args, dist):
            "data": "synthetic", "steps": K, "warmup": W,
            "config": {"workload": f"elastic velocity-stress gradient 1024x2048, dx 2 m, nt {nt}, "
                                   f"{len(rix)} vertical-strain receivers, 5 Hz, checkpointed",
-                      "adjoint": args.el_adjoint},
+                      "adjoint": args.el_adjoint, "tiles": args.el_tiles},
            "s_per_shot": sum(times) / K, "device_ms_forward": statistics.mean(fwd_ms),
            "device_ms_gradient": statistics.mean(grad_ms),
            "counted_points_per_shot": pts}
@@ -742,12 +744,12 @@ def run_interferometry(args, dist):
 def run_small(args, dist):
     """Small plain RTM (150 x 400, dx 10 m, nt 2000, 20 shots x 400 receivers, interval 2):
     the whole TSWRTMEngine.migrate_multiple_shots call (20 shots, stack, post-stack) on
-    the GPU, the same 20 shots as one BatchEngine batch (every launch advances all shots;
-    host stack in shot order, bit-identical to the serial stack), and the reference's
-    CPU path (oracle port of wave2d.c + its Python loops) over the same 20 shots on all
-    host cores.  Observed gathers: forward modelling in the true model on the GPU."""
-    from das_gb300.batch import BatchEngine, ShotJob
-    from das_gb300.rtm_engine import TSWRTMEngine, post_stack
+    the GPU in its default form (grids this small run their shots as one batch: every
+    launch advances all shots, images stacked in shot order) and as the plain per-shot
+    loop (batch="off"), and the reference's CPU path (oracle port of wave2d.c + its
+    Python loops) over the same 20 shots on all host cores.  Observed gathers: forward
+    modelling in the true model on the GPU."""
+    from das_gb300.rtm_engine import TSWRTMEngine
     from das_gb300.synthetic import plain_small
     from das_gb300.velocity_flood import FloodModels
     from das_gb300.wave_solver import WaveSolver2D
@@ -758,41 +760,26 @@ def run_small(args, dist):
     gathers = [solver.forward_propagate_acoustic(sv.vel_true, sv.wavelet, int(s), sv.src_iz,
                                                  sv.rec_ix, sv.rec_iz)[0] for s in sv.src_ix]
     fm = FloodModels(sv.vel_true, sv.vel_mig, sv.vel_mig, 0, 0)
-    eng = TSWRTMEngine(solver)
     waves = [sv.wavelet] * n
     siz = [sv.src_iz] * n
+    timing = {}
+    results = {}
+    for mode in ("off", "auto"):
+        eng = TSWRTMEngine(solver, batch=mode)
 
-    def serial():
-        return eng.migrate_multiple_shots(fm, waves, list(sv.src_ix), siz, gathers, sv.rec_ix,
-                                          sv.rec_iz, 2)
+        def survey():
+            return eng.migrate_multiple_shots(fm, waves, list(sv.src_ix), siz, gathers,
+                                              sv.rec_ix, sv.rec_iz, 2)
 
-    for _ in range(args.warmup):
-        serial()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res = serial()
-    serial_s = (time.perf_counter() - t0) / args.steps
-    jobs = [ShotJob(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.vel_mig, sv.vel_mig, sv.wavelet,
-                    gathers[k], sv.rec_ix, int(sv.src_ix[k]), sv.src_iz, sv.rec_iz, 2,
-                    sv.n_sponge, sv.sponge_alpha) for k in range(n)]
-    be = BatchEngine(arena_bytes=4 << 30, max_shots=n, tile=(4, 4))
-
-    def batched():
-        out, st = be.run(jobs)
-        stacked = np.zeros((sv.nz, sv.nx), np.float32)
-        illum = np.zeros((sv.nz, sv.nx), np.float32)
-        for img, ill in out:
-            stacked += img
-            illum += ill
-        return post_stack(solver, stacked, illum), st
-
-    for _ in range(args.warmup):
-        batched()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        bres, bst = batched()
-    batch_s = (time.perf_counter() - t0) / args.steps
-    same = bool(np.array_equal(bres.raw_image, res.raw_image))
+        for _ in range(args.warmup):
+            survey()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            results[mode] = survey()
+        timing[mode] = (time.perf_counter() - t0) / args.steps
+        eng.close()
+    same = all(np.array_equal(getattr(results["auto"], f), getattr(results["off"], f))
+               for f in ("raw_image", "laplacian_image", "normalized_image"))
     pts = n * sv.counted_points_per_shot()
     cpu = None
     if args.small_cpu_shots > 0:
@@ -811,16 +798,15 @@ def run_small(args, dist):
         cpu = {"value": k * sv.counted_points_per_shot() / cpu_s / 1e9, "unit": UNIT,
                "cores": threads, "kind": kind,
                "sample": f"migrate_multiple_shots over {k} of the {n} shots, {cpu_s:.1f} s"}
-    out = {"metric": METRIC, "value": pts / batch_s / 1e9, "unit": UNIT, "n_gpus": 1,
+    out = {"metric": METRIC, "value": pts / timing["auto"] / 1e9, "unit": UNIT, "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
            "dtype": "f32", "data": "synthetic",
            "config": {"workload": sv.name, "nz": sv.nz, "nx": sv.nx, "nt": sv.nt, "shots": n,
-                      "interval": 2},
-           "s_per_survey_batched": batch_s, "s_per_survey_serial": serial_s,
-           "gpts_per_s_serial": pts / serial_s / 1e9, "shots_per_s_batched": n / batch_s,
-           "shots_per_s_serial": n / serial_s, "batched_device_ms": bst["device_ms"],
-           "batched_stack_equals_serial": same, "cpu_baseline": cpu}
-    be.close()
+                      "interval": 2, "timed": "migrate_multiple_shots with host arrays"},
+           "s_per_survey": timing["auto"], "s_per_survey_per_shot_loop": timing["off"],
+           "gpts_per_s_per_shot_loop": pts / timing["off"] / 1e9,
+           "shots_per_s": n / timing["auto"], "shots_per_s_per_shot_loop": n / timing["off"],
+           "batched_equals_per_shot_loop": same, "cpu_baseline": cpu}
     solver.close()
     print(json.dumps(out), flush=True)
 
@@ -833,6 +819,7 @@ def main():
     ap.add_argument("--xc-windows", type=int, default=32)
     ap.add_argument("--el-nt", type=int, default=6000)
     ap.add_argument("--el-adjoint", default="tiled", choices=["tiled", "cells"])
+    ap.add_argument("--el-tiles", default="4,4:4,2")  # step warps,rows : adjoint warps,rows
     ap.add_argument("--small-cpu-shots", type=int, default=20)
     ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])

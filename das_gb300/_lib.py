@@ -58,6 +58,8 @@ _SIGS = {
                                  c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     "w2d_stack_reset": (c_int, [c_void_p]),
     "w2d_stack_read": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "w2d_stack_add": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "w2d_device_memory": (c_int, [ctypes.POINTER(c_ull), ctypes.POINTER(c_ull)]),
     "w2d_post_stack": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "w2d_shot_stage": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int]),
     "w2d_migrate_staged": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int, c_int,
@@ -86,6 +88,7 @@ _SIGS = {
     "w2d_elastic_gradient_batch": (c_int, [c_void_p] * 6),
     "w2d_elastic_shot_bytes": (c_ull, [c_int, c_int, c_int, c_int]),
     "w2d_elastic_set_adjoint": (c_int, [c_void_p, c_int]),
+    "w2d_elastic_set_tiles": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
@@ -155,3 +158,10 @@ def check(rc: int) -> None:
     if rc != 0:
         msg = _LIB.w2d_last_error() if _LIB is not None else b""
         raise W2DError(rc, (msg or b"").decode(errors="replace"))
+
+
+def device_memory():
+    """(free, total) bytes of device memory."""
+    f, t = c_ull(), c_ull()
+    check(load().w2d_device_memory(ctypes.byref(f), ctypes.byref(t)))
+    return int(f.value), int(t.value)

@@ -347,53 +347,88 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-constexpr int EL_ADJ_WARPS = 4, EL_ADJ_RPW = 2;
+constexpr int EL_ADJ_WARPS = 4, EL_ADJ_RPW = 2;  // default tile: 128 x 8
 
-inline cudaError_t launch_el_adj_a(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
-                                   const ElStrides& sd, const ElState& a, const ElState& r,
-                                   float* glam, float* gmu, float* gbx, float* gbz, unsigned* err,
-                                   int n_shots, cudaStream_t st)
+inline bool el_adj_tile_supported(int warps, int rpw)
 {
-    using T = ElAdjTile<EL_ADJ_WARPS, EL_ADJ_RPW>;
+    return (warps == 4 && (rpw == 2 || rpw == 1)) || (warps == 8 && rpw == 1);
+}
+
+template <int WARPS, int RPW>
+cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
+                              const ElStrides& sd, const ElState& a, const ElState& r, float* glam,
+                              float* gmu, float* gbx, float* gbz, unsigned* err, int n_shots,
+                              cudaStream_t st)
+{
+    using T = ElAdjTile<WARPS, RPW>;
     const int bytes = 8 * T::BOX * 4 + 128;
-    static bool attr_set = false;  // one attribute call per process
+    static bool attr_set = false;  // one attribute call per process and shape
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(el_adj_a<EL_ADJ_WARPS, EL_ADJ_RPW>,
+        cudaError_t e = cudaFuncSetAttribute(el_adj_a<WARPS, RPW>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    el_adj_a<EL_ADJ_WARPS, EL_ADJ_RPW><<<grid, EL_ADJ_WARPS * 32, bytes, st>>>(
-        m, g, p, sd, a, r, glam, gmu, gbx, gbz, err);
+    el_adj_a<WARPS, RPW><<<grid, WARPS * 32, bytes, st>>>(m, g, p, sd, a, r, glam, gmu, gbx, gbz,
+                                                          err);
     return cudaGetLastError();
+}
+
+template <int WARPS, int RPW>
+cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
+                              const ElStrides& sd, const ElState& a, const ElState& t,
+                              int then_k1, unsigned* err, int n_shots, cudaStream_t st)
+{
+    using T = ElAdjTile<WARPS, RPW>;
+    const int bytes = 2 * T::BOX * 4 + 128;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(el_adj_b<WARPS, RPW>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
+    el_adj_b<WARPS, RPW><<<grid, WARPS * 32, bytes, st>>>(m, g, p, sd, a, t, then_k1, err);
+    return cudaGetLastError();
+}
+
+// Pass A / pass B on tiles of `warps` x `rpw` rows (maps with box height warps*rpw + 4).
+inline cudaError_t launch_el_adj_a(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
+                                   const ElStrides& sd, const ElState& a, const ElState& r,
+                                   float* glam, float* gmu, float* gbx, float* gbz, unsigned* err,
+                                   int n_shots, cudaStream_t st, int warps = EL_ADJ_WARPS,
+                                   int rpw = EL_ADJ_RPW)
+{
+    if (warps == 4 && rpw == 2)
+        return launch_el_adj_a_t<4, 2>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+    if (warps == 4 && rpw == 1)
+        return launch_el_adj_a_t<4, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+    if (warps == 8 && rpw == 1)
+        return launch_el_adj_a_t<8, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+    return cudaErrorInvalidValue;
 }
 
 inline cudaError_t launch_el_adj_b(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                                    const ElStrides& sd, const ElState& a, const ElState& t,
-                                   int then_k1, unsigned* err, int n_shots, cudaStream_t st)
+                                   int then_k1, unsigned* err, int n_shots, cudaStream_t st,
+                                   int warps = EL_ADJ_WARPS, int rpw = EL_ADJ_RPW)
 {
-    using T = ElAdjTile<EL_ADJ_WARPS, EL_ADJ_RPW>;
-    const int bytes = 2 * T::BOX * 4 + 128;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(el_adj_b<EL_ADJ_WARPS, EL_ADJ_RPW>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    el_adj_b<EL_ADJ_WARPS, EL_ADJ_RPW><<<grid, EL_ADJ_WARPS * 32, bytes, st>>>(m, g, p, sd, a, t,
-                                                                             then_k1, err);
-    return cudaGetLastError();
+    if (warps == 4 && rpw == 2)
+        return launch_el_adj_b_t<4, 2>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+    if (warps == 4 && rpw == 1)
+        return launch_el_adj_b_t<4, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+    if (warps == 8 && rpw == 1)
+        return launch_el_adj_b_t<8, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+    return cudaErrorInvalidValue;
 }
 
-// 3D map over the states (5 planes per shot) of a buffer, with this file's box.
+// 3D map over the states (5 planes per shot) of a buffer, with boxes of tile height tz.
 inline int make_el_adj_map(CUtensorMap* m, const float* base, int nx, int nz, int ldx,
-                           size_t plane, int n_shots)
+                           size_t plane, int n_shots, int tz = EL_ADJ_WARPS * EL_ADJ_RPW)
 {
-    return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW,
-                              ElAdjTile<EL_ADJ_WARPS, EL_ADJ_RPW>::TZ + 4);
+    return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW, tz + 4);
 }
 
 }  // namespace w2d

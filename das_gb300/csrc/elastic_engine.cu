@@ -60,6 +60,11 @@ struct w2d_elastic {
     CUtensorMap map_state;                  // 3D map over the S x 5 planes of `state`
     std::vector<CUtensorMap> seg_maps;      // one per slot of `seg`
     int adj_form = 1;                       // 1: TMA-tiled adjoint passes, 0: per-cell kernels
+    int fwd_warps = EL_WARPS, fwd_rpw = EL_RPW;          // step kernels' tile
+    int adj_warps = EL_ADJ_WARPS, adj_rpw = EL_ADJ_RPW;  // adjoint passes' tile
+    // the tiles the current maps were made for (a change applies at the next forward)
+    int map_fwd_warps = EL_WARPS, map_fwd_rpw = EL_RPW, map_adj_warps = EL_ADJ_WARPS,
+        map_adj_rpw = EL_ADJ_RPW;
     CUtensorMap adj_map_tmp;                // the adjoint passes' maps (their own box height)
     std::vector<CUtensorMap> adj_seg_maps;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -138,7 +143,8 @@ int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, c
     st.nt = e->nt;
     st.n = n;
     st.err = e->err;
-    W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st, e->S));
+    W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st, e->S, e->map_fwd_warps,
+                                     e->map_fwd_rpw));
     return W2D_OK;
 }
 
@@ -277,15 +283,23 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
         (rc = grow(&e->ckpt, (size_t)e->n_seg * S * SS, &e->ckpt_cap)) ||
         (rc = grow(&e->seg, (size_t)(e->seg_len + 1) * S * SS, &e->seg_cap)))
         return rc;
-    if ((rc = make_el_state_map(&e->map_state, e->state, e->nx, e->nz, e->ldx, P, S))) return rc;
+    e->map_fwd_warps = e->fwd_warps;
+    e->map_fwd_rpw = e->fwd_rpw;
+    e->map_adj_warps = e->adj_warps;
+    e->map_adj_rpw = e->adj_rpw;
+    const int ftz = e->fwd_warps * e->fwd_rpw, atz = e->adj_warps * e->adj_rpw;
+    if ((rc = make_el_state_map(&e->map_state, e->state, e->nx, e->nz, e->ldx, P, S, ftz)))
+        return rc;
     e->seg_maps.resize(e->seg_len + 1);
     for (int i = 0; i <= e->seg_len; ++i)
-        if ((rc = make_el_state_map(&e->seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S)))
+        if ((rc = make_el_state_map(&e->seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S, ftz)))
             return rc;
-    if ((rc = make_el_adj_map(&e->adj_map_tmp, e->tmp, e->nx, e->nz, e->ldx, P, S))) return rc;
+    if ((rc = make_el_adj_map(&e->adj_map_tmp, e->tmp, e->nx, e->nz, e->ldx, P, S, atz)))
+        return rc;
     e->adj_seg_maps.resize(e->seg_len + 1);
     for (int i = 0; i <= e->seg_len; ++i)
-        if ((rc = make_el_adj_map(&e->adj_seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S)))
+        if ((rc = make_el_adj_map(&e->adj_seg_maps[i], e->slot(i), e->nx, e->nz, e->ldx, P, S,
+                                  atz)))
             return rc;
     const size_t hp = (size_t)e->nx * 4, dp = (size_t)e->ldx * 4, np = (size_t)e->nx * e->nz;
     const float* src[4] = {lam, mu, bx, bz};
@@ -397,9 +411,9 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 m.f_next = e->adj_seg_maps[n + 1 - a0];
                 m.f_curr = e->adj_seg_maps[n - a0];
                 W2D_CUDA_TRY(launch_el_adj_a(m, g, prm, sd, a, r, glam, gmu, gbx, gbz, e->err, S,
-                                             e->st));
+                                             e->st, e->map_adj_warps, e->map_adj_rpw));
                 W2D_CUDA_TRY(launch_el_adj_b(m, g, prm, sd, a, t, n >= 1 ? 1 : 0, e->err, S,
-                                             e->st));
+                                             e->st, e->map_adj_warps, e->map_adj_rpw));
             } else {
                 ElState f_next = e->S0(e->slot(n + 1 - a0));  // u_{n+1}
                 ElState f_curr = e->S0(e->slot(n - a0));      // u_n
@@ -444,6 +458,21 @@ int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
 {
     W2D_CHECK_ARG(e && (form == 0 || form == 1), "form must be 0 (per-cell) or 1 (tiled)");
     e->adj_form = form;
+    return W2D_OK;
+}
+
+int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp,
+                          int adjoint_warps, int adjoint_rows_per_warp)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CHECK_ARG(el_tile_supported(step_warps, step_rows_per_warp),
+                  "step tile must be 4x4, 4x2, 8x2 or 8x1 (warps x rows per warp)");
+    W2D_CHECK_ARG(el_adj_tile_supported(adjoint_warps, adjoint_rows_per_warp),
+                  "adjoint tile must be 4x2, 4x1 or 8x1 (warps x rows per warp)");
+    e->fwd_warps = step_warps;
+    e->fwd_rpw = step_rows_per_warp;
+    e->adj_warps = adjoint_warps;
+    e->adj_rpw = adjoint_rows_per_warp;
     return W2D_OK;
 }
 

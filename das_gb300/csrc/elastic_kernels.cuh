@@ -385,39 +385,58 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-constexpr int EL_WARPS = 4, EL_RPW = 4;
+constexpr int EL_WARPS = 4, EL_RPW = 4;  // default tile: 4 warps x 4 rows (128 x 16)
 
-// The 3D tensor map of the 5-plane states of n_shots shots stored one after another.
-inline int make_el_state_map(CUtensorMap* m, const float* base, int nx, int nz, int ldx,
-                             size_t plane, int n_shots = 1)
+// Tile shapes the step kernels are built for (warps per CTA x rows per warp).
+inline bool el_tile_supported(int warps, int rpw)
 {
-    return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW,
-                              ElTile<EL_WARPS, EL_RPW>::TZ + 4);
+    return (warps == 4 && (rpw == 4 || rpw == 2)) || (warps == 8 && (rpw == 2 || rpw == 1));
 }
 
-// Velocity then stress phase of one step of n_shots shots (src -> dst; src == dst
-// updates in place).
-inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, const ElStep& s,
-                                       cudaStream_t st, int n_shots = 1)
+// The 3D tensor map of the 5-plane states of n_shots shots stored one after another,
+// with boxes of tile height tz (+ 4 halo rows).
+inline int make_el_state_map(CUtensorMap* m, const float* base, int nx, int nz, int ldx,
+                             size_t plane, int n_shots = 1, int tz = EL_WARPS * EL_RPW)
 {
-    using T = ElTile<EL_WARPS, EL_RPW>;
+    return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW, tz + 4);
+}
+
+template <int WARPS, int RPW>
+cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElStep& s,
+                                  cudaStream_t st, int n_shots)
+{
+    using T = ElTile<WARPS, RPW>;
     const int vbytes = 3 * T::BOX * 4 + 128, sbytes = 2 * T::BOX * 4 + 128;
-    static bool attr_set = false;  // one attribute call per process
+    static bool attr_set = false;  // one attribute call per process and shape
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(elastic_velocity_kernel<EL_WARPS, EL_RPW>,
+        cudaError_t e = cudaFuncSetAttribute(elastic_velocity_kernel<WARPS, RPW>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, vbytes);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(elastic_stress_kernel<EL_WARPS, EL_RPW>,
+            e = cudaFuncSetAttribute(elastic_stress_kernel<WARPS, RPW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    elastic_velocity_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, vbytes, st>>>(maps, g, s);
+    elastic_velocity_kernel<WARPS, RPW><<<grid, WARPS * 32, vbytes, st>>>(maps, g, s);
     ElStep s2 = s;
     s2.src_pos = nullptr;
-    elastic_stress_kernel<EL_WARPS, EL_RPW><<<grid, EL_WARPS * 32, sbytes, st>>>(maps, g, s2);
+    elastic_stress_kernel<WARPS, RPW><<<grid, WARPS * 32, sbytes, st>>>(maps, g, s2);
     return cudaGetLastError();
+}
+
+// Velocity then stress phase of one step of n_shots shots (src -> dst; src == dst
+// updates in place), on tiles of `warps` x `rpw` rows; the maps' box height must be
+// warps * rpw + 4.
+inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, const ElStep& s,
+                                       cudaStream_t st, int n_shots = 1, int warps = EL_WARPS,
+                                       int rpw = EL_RPW)
+{
+    if (warps == 4 && rpw == 4) return launch_elastic_step_t<4, 4>(g, maps, s, st, n_shots);
+    if (warps == 4 && rpw == 2) return launch_elastic_step_t<4, 2>(g, maps, s, st, n_shots);
+    if (warps == 8 && rpw == 2) return launch_elastic_step_t<8, 2>(g, maps, s, st, n_shots);
+    if (warps == 8 && rpw == 1) return launch_elastic_step_t<8, 1>(g, maps, s, st, n_shots);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace w2d

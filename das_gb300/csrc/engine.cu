@@ -933,6 +933,16 @@ void w2d_host_free(void* p)
     if (p) cudaFreeHost(p);
 }
 
+int w2d_device_memory(unsigned long long* free_bytes, unsigned long long* total_bytes)
+{
+    W2D_CHECK_ARG(free_bytes && total_bytes, "NULL argument");
+    size_t f = 0, t = 0;
+    W2D_CUDA_TRY(cudaMemGetInfo(&f, &t));
+    *free_bytes = f;
+    *total_bytes = t;
+    return W2D_OK;
+}
+
 int w2d_stack_reset(w2d_engine* e)
 {
     W2D_CHECK_ARG(e, "engine is NULL");
@@ -941,6 +951,21 @@ int w2d_stack_reset(w2d_engine* e)
     W2D_CUDA_TRY(cudaMemsetAsync(e->stack_img.p, 0, e->plane * 4, e->stream));
     W2D_CUDA_TRY(cudaMemsetAsync(e->stack_ill.p, 0, e->plane * 4, e->stream));
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    return W2D_OK;
+}
+
+int w2d_stack_add(w2d_engine* e, const float* image, const float* illum)
+{
+    W2D_CHECK_ARG(e && image && illum, "NULL argument");
+    W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
+    int rc;
+    if ((rc = e->image.ensure(e->plane)) || (rc = e->illum.ensure(e->plane))) return rc;
+    if ((rc = upload_field(e, e->image.p, image)) || (rc = upload_field(e, e->illum.p, illum)))
+        return rc;
+    add_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->stack_img.p, e->image.p, e->plane);
+    add_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->stack_ill.p, e->illum.p, e->plane);
+    W2D_CUDA_TRY(cudaGetLastError());
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));  // the caller's arrays are free to go
     return W2D_OK;
 }
 

@@ -8,7 +8,10 @@
   wavefield never leaves the device (kept whole, or checkpointed and recomputed).
 * ``TSWRTMEngine.migrate_multiple_shots``  rtm_engine.py:106-171: the shot images are
   stacked on the device; sponge mute, illumination normalisation and the Laplacian
-  run on the stacked image as the reference does.
+  run on the stacked image as the reference does.  On grids too small for one shot
+  to fill the GPU the shots run as one batch (every launch advances all of them,
+  das_gb300.batch); their images are stacked in shot order, so the result is the
+  same bit for bit.
 """
 from __future__ import annotations
 
@@ -26,6 +29,8 @@ __all__ = ["RTMResult", "apply_laplacian_filter", "TSWRTMEngine", "FloodModels",
            "ricker_wavelet"]
 
 _STORAGE = {"auto": 0, "all": 1, "checkpoint": 2}
+# below this many grid points one shot's step launch leaves most of the GPU idle
+_BATCH_POINTS = 1 << 21
 
 
 @dataclass
@@ -51,17 +56,33 @@ def apply_laplacian_filter(image: np.ndarray, dx: float, dz: float) -> np.ndarra
 class TSWRTMEngine:
     """Transmitted surface-wave reverse-time migration on one GB300."""
 
-    def __init__(self, solver: WaveSolver2D, storage: str = "auto"):
+    def __init__(self, solver: WaveSolver2D, storage: str = "auto", batch: str = "auto"):
         if storage not in _STORAGE:
             raise ValueError(f"storage must be one of {sorted(_STORAGE)}")
+        if batch not in ("auto", "on", "off"):
+            raise ValueError("batch must be 'auto', 'on' or 'off'")
         self.solver = solver
         self.storage = storage
+        self.batch = batch
+        self._batch_engine = None
+        self._batch_arena = 0
+
+    def close(self):
+        if self._batch_engine is not None:
+            self._batch_engine.close()
+            self._batch_engine = None
+            self._batch_arena = 0
 
     def _prepare(self, flood_models, receiver_data, receiver_ix, receiver_iz, source_ts,
                  source_ix, source_iz):
         s = self.solver
         s._set_velocity(0, flood_models.sediment_flood)
         s._set_velocity(1, flood_models.rock_flood)
+        return self._check(receiver_data, receiver_ix, receiver_iz, source_ts, source_ix,
+                           source_iz)
+
+    def _check(self, receiver_data, receiver_ix, receiver_iz, source_ts, source_ix, source_iz):
+        s = self.solver
         w = np.ascontiguousarray(source_ts, dtype=np.float32).reshape(-1)
         data = np.ascontiguousarray(receiver_data, dtype=np.float32)
         if data.ndim != 2:
@@ -101,13 +122,12 @@ class TSWRTMEngine:
         s = self.solver
         eng = s._eng()
         _lib.check(s._lib.w2d_stack_reset(eng))
-        for k in range(len(source_coords_ix)):
-            w, data, rix, riz, six, siz = self._prepare(
-                flood_models, receiver_gathers[k], receiver_ix, receiver_iz, source_waveforms[k],
-                source_coords_ix[k], source_coords_iz[k])
-            _lib.check(s._lib.w2d_migrate_shot(
-                eng, w.ctypes.data, len(w), six, siz, data.ctypes.data, rix.ctypes.data,
-                data.shape[1], riz, int(snapshot_interval), _STORAGE[self.storage], None, None))
+        if not (self._use_batch(len(source_coords_ix)) and self._migrate_batched(
+                eng, flood_models, source_waveforms, source_coords_ix, source_coords_iz,
+                receiver_gathers, receiver_ix, receiver_iz, snapshot_interval)):
+            self._migrate_serial(eng, flood_models, source_waveforms, source_coords_ix,
+                                 source_coords_iz, receiver_gathers, receiver_ix, receiver_iz,
+                                 snapshot_interval)
         # mute, normalisation and Laplacian run on the device stack
         raw, lap, norm = (np.empty((s.nz, s.nx), np.float32) for _ in range(3))
         _lib.check(s._lib.w2d_post_stack(eng, 1 if mute_sponge else 0, raw.ctypes.data,
@@ -115,6 +135,58 @@ class TSWRTMEngine:
         return RTMResult(raw_image=raw, laplacian_image=lap, normalized_image=norm,
                          grid_x=np.arange(s.nx) * s.dx, grid_z=np.arange(s.nz) * s.dz,
                          dx=s.dx, dz=s.dz)
+
+    def _use_batch(self, n_shots: int) -> bool:
+        if self.batch == "off" or n_shots < 2:
+            return False
+        s = self.solver
+        if s.sponge is not None and not np.array_equal(s.sponge, s._default_sponge()):
+            return False  # a caller-modified sponge: the batch engine builds the Cerjan one
+        if self.batch == "on":
+            return True
+        return self.storage == "auto" and s.nx * s.nz <= _BATCH_POINTS
+
+    def _migrate_batched(self, eng, flood_models, source_waveforms, source_coords_ix,
+                         source_coords_iz, receiver_gathers, receiver_ix, receiver_iz,
+                         snapshot_interval) -> bool:
+        """All shots as one batch; False (nothing done) when one shot does not fit."""
+        from .batch import BatchEngine, ShotJob
+        s = self.solver
+        n_sp = s.n_sponge if s.sponge is not None else -1
+        jobs = []
+        for k in range(len(source_coords_ix)):
+            w, data, rix, riz, six, siz = self._check(receiver_gathers[k], receiver_ix,
+                                                      receiver_iz, source_waveforms[k],
+                                                      source_coords_ix[k], source_coords_iz[k])
+            jobs.append(ShotJob(s.nx, s.nz, s.dx, s.dz, s.dt, flood_models.sediment_flood,
+                                flood_models.rock_flood, w, data, rix, six, siz, riz,
+                                int(snapshot_interval), n_sp, s.sponge_alpha,
+                                bool(s.free_surface_top)))
+        per = max(BatchEngine.shot_bytes(j) for j in jobs)
+        free, _ = _lib.device_memory()
+        arena = min(per * len(jobs), int(0.5 * free) + self._batch_arena)
+        if arena < per:
+            return False
+        if self._batch_engine is None or self._batch_arena < arena:
+            self.close()
+            self._batch_engine = BatchEngine(arena_bytes=arena, max_shots=len(jobs), tile=(4, 4))
+            self._batch_arena = arena
+        results, _ = self._batch_engine.run(jobs)
+        for img, ill in results:  # shot order, as the serial stack
+            _lib.check(s._lib.w2d_stack_add(eng, img.ctypes.data, ill.ctypes.data))
+        return True
+
+    def _migrate_serial(self, eng, flood_models, source_waveforms, source_coords_ix,
+                        source_coords_iz, receiver_gathers, receiver_ix, receiver_iz,
+                        snapshot_interval):
+        s = self.solver
+        for k in range(len(source_coords_ix)):
+            w, data, rix, riz, six, siz = self._prepare(
+                flood_models, receiver_gathers[k], receiver_ix, receiver_iz, source_waveforms[k],
+                source_coords_ix[k], source_coords_iz[k])
+            _lib.check(s._lib.w2d_migrate_shot(
+                eng, w.ctypes.data, len(w), six, siz, data.ctypes.data, rix.ctypes.data,
+                data.shape[1], riz, int(snapshot_interval), _STORAGE[self.storage], None, None))
 
 
 def post_stack(solver: WaveSolver2D, stacked: np.ndarray, illum: np.ndarray,

@@ -59,6 +59,7 @@ class WaveSolver2D:
         self.sponge = np.ones((nz, nx), dtype=np.float32)
         self._lib.build_cerjan_sponge(self.sponge.ctypes.data, nx, nz, n_sponge, sponge_alpha,
                                       1 if free_surface_top else 0)
+        self._sponge0 = self.sponge.copy()
         self._engine = None
         self._engine_sponge = None
         self.storage = "auto"
@@ -67,6 +68,10 @@ class WaveSolver2D:
         # step launch: one CTA per tile ("grid") or persistent CTAs ("persistent");
         # each optionally a programmatic dependent of the previous step (pdl)
         self.launch = ("grid", True)
+
+    def _default_sponge(self) -> np.ndarray:
+        """The Cerjan sponge of this grid's (n_sponge, sponge_alpha) as built at creation."""
+        return self._sponge0
 
     # -- engine handle -----------------------------------------------------------
     def _eng(self):

@@ -133,6 +133,9 @@ int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, in
 /* Device stack of migrated shots (rtm_engine.py:142-143). */
 int w2d_stack_reset(w2d_engine* e);
 int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out);
+/* Add one shot's (image, illumination), HOST (nz, nx) arrays, to the device stack
+ * (float32 adds in call order, as rtm_engine.py:142-143 stacks). */
+int w2d_stack_add(w2d_engine* e, const float* image, const float* illum);
 /* Post-stack of the device stack (rtm_engine.py:145-158) on the device: mute where the
  * sponge is below 0.99, illumination normalisation with eps = 1e-4 * max, 3x3
  * Laplacian with symmetric edges; the three (nz, nx) images are copied out. */
@@ -157,6 +160,9 @@ int w2d_engine_timer_stop(w2d_engine* e, float* ms);
 int w2d_set_device(int device);
 /* PCI bus id ("0000:xx:00.0") of the current device, for per-GPU monitoring. */
 int w2d_device_pci_bus_id(char* buf, int len);
+
+/* Free and total device memory of the current device, in bytes. */
+int w2d_device_memory(unsigned long long* free_bytes, unsigned long long* total_bytes);
 
 /* Page-locked host memory for fast host<->device copies of shot inputs/outputs. */
 int w2d_host_alloc(void** out, unsigned long long bytes);
@@ -209,6 +215,11 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
 /* How the adjoint passes run: 1 (default) TMA-tiled passes, 0 per-cell kernels.
  * The two agree to float32 rounding (contraction differs); both are exact adjoints. */
 int w2d_elastic_set_adjoint(w2d_elastic* e, int form);
+/* Tile shapes (warps per CTA x rows per warp, 128 columns wide) of the step kernels
+ * (4x4 default, 4x2, 8x2, 8x1) and of the tiled adjoint passes (4x2 default, 4x1,
+ * 8x1); applies from the next forward call.  Results do not depend on the tiles. */
+int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp,
+                          int adjoint_warps, int adjoint_rows_per_warp);
 /* Device bytes one shot of a batch holds (checkpoints, one recomputed segment, fields). */
 unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 

@@ -148,3 +148,26 @@ def test_tiled_adjoint_equals_per_cell_adjoint(nz, nx, free_surface):
     rel = np.linalg.norm(a - b) / np.linalg.norm(b)
     print(f"{nz} x {nx}: tiled vs per-cell adjoint rel L2 {rel:.2e}")
     assert rel < 1e-5
+
+
+def test_tile_shapes_do_not_change_results():
+    """Every supported step tile gives the same traces bit for bit (the step's float32
+    operation order is fixed); every adjoint tile the same gradient to rounding."""
+    from das_gb300.elastic import elastic_traces
+    torch, solver, grid, w, rix = _setup()
+    vs, _ = _model()
+    R = torch.tensor(np.random.default_rng(4).standard_normal((len(w), len(rix))).astype(np.float32),
+                     device="cuda")
+    out = {}
+    for step, adj in [((4, 4), (4, 2)), ((4, 2), (4, 1)), ((8, 2), (8, 1)), ((8, 1), (4, 2))]:
+        solver.set_tiles(step, adj)
+        v = torch.tensor(vs, device="cuda", requires_grad=True)
+        d = elastic_traces(v, solver, w, 20, 3, rix, 2)
+        (d * R).sum().backward()
+        out[(step, adj)] = (d.detach().cpu().numpy(), v.grad.cpu().numpy().astype(np.float64))
+    d0, g0 = out[((4, 4), (4, 2))]
+    for k, (d, g) in out.items():
+        np.testing.assert_array_equal(d, d0)
+        assert np.linalg.norm(g - g0) <= 1e-6 * np.linalg.norm(g0), k
+    with pytest.raises(Exception):
+        solver.set_tiles((3, 3), (4, 2))

@@ -163,12 +163,15 @@ def test_migrate_shot_golden(golden, storage):
     _close(ill, g["ms_illum"], IMG_TOL, what="illumination")
 
 
-def test_migrate_multiple_golden(golden):
+@pytest.mark.parametrize("batch", ["off", "on"])
+def test_migrate_multiple_golden(golden, batch):
+    """The serial shot loop and the batched form (all shots advanced by the same
+    launches, stacked in shot order), both against the reference's golden stack."""
     from das_gb300.rtm_engine import TSWRTMEngine
     from das_gb300.velocity_flood import FloodModels
     g = golden("loops")
     s = _solver(_grid(g))
-    eng = TSWRTMEngine(s)
+    eng = TSWRTMEngine(s, batch=batch)
     fm = FloodModels(g["vtrue"], g["vsmooth"], g["vsmooth"], 0, 0)
     res = eng.migrate_multiple_shots(fm, [g["wavelet"]] * 3, list(g["mm_src_ix"]), [2] * 3,
                                      list(g["mm_gathers"]), np.arange(s.nx), 2, 2)
@@ -177,6 +180,39 @@ def test_migrate_multiple_golden(golden):
     # scipy's convolve2d (the reference's Laplacian, also used here) rounds
     # differently by an ulp between x86-64 and aarch64 builds: tolerance only
     _close(res.laplacian_image, g["mm_lap"], IMG_TOL, exact=False, what="laplacian")
+    eng.close()
+
+
+def test_migrate_multiple_batched_equals_serial():
+    """Twelve shots with a caller-chosen interval and receivers on a row below the
+    surface: the batched form's three images bit-identical to the serial loop's; a
+    caller-modified sponge makes the batched form step aside (same result)."""
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D, ricker_wavelet
+    nz, nx, dt = 90, 260, 1e-3
+    rng = np.random.default_rng(12)
+    vel = rng.uniform(1600, 2600, (nz, nx)).astype(np.float32)
+    w, _ = ricker_wavelet(8.0, dt, 0.4)
+    s = WaveSolver2D(nx, nz, 10.0, 10.0, dt, n_sponge=20)
+    fm = FloodModels(vel, vel, (vel * 1.02).astype(np.float32), 0, 0)
+    rix = np.arange(3, nx - 3, 2)
+    gathers = [(rng.standard_normal((len(w), len(rix))) * 1e-3).astype(np.float32)
+               for _ in range(12)]
+    six = list(np.linspace(5, nx - 6, 12).astype(int))
+    out = {}
+    for mode in ("off", "on"):
+        eng = TSWRTMEngine(s, batch=mode)
+        out[mode] = eng.migrate_multiple_shots(fm, [w] * 12, six, [3] * 12, gathers, rix, 4, 3)
+        eng.close()
+    for f in ("raw_image", "laplacian_image", "normalized_image"):
+        np.testing.assert_array_equal(getattr(out["on"], f), getattr(out["off"], f))
+    assert np.abs(out["on"].raw_image).max() > 0
+    s.sponge = s.sponge.copy()
+    s.sponge[:, :5] *= 0.5
+    eng = TSWRTMEngine(s, batch="on")
+    assert not eng._use_batch(12)
+    eng.close()
 
 
 # ---- engine vs live oracle over shapes, tiles and intervals ----------------------------
