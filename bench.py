@@ -819,7 +819,7 @@ def main():
     ap.add_argument("--xc-windows", type=int, default=32)
     ap.add_argument("--el-nt", type=int, default=6000)
     ap.add_argument("--el-adjoint", default="tiled", choices=["tiled", "cells"])
-    ap.add_argument("--el-tiles", default="4,4:4,2")  # step warps,rows : adjoint warps,rows
+    ap.add_argument("--el-tiles", default="4,2:4,1")  # step warps,rows : adjoint warps,rows
     ap.add_argument("--small-cpu-shots", type=int, default=20)
     ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])

@@ -250,19 +250,26 @@ class BatchEngine:
                 running[slot] = pending.pop(0)
 
         admit()
+        flying = False
         while running or pending:
             if not running:
                 admit()
                 if not running:
                     raise MemoryError("a shot does not fit in the arena even when it is empty")
             max_active = max(max_active, len(running))
-            self.launch()
+            if not flying:
+                self.launch()
             admit()  # uploads overlap the replay in flight; these shots join the next one
             self.wait()
             dev_ms += self.last_ms
             pts += self.last_points
             launches += self.last_launches
-            for slot in [s for s in running if self.finished(s)]:
+            fin = [s for s in running if self.finished(s)]
+            # the next replay runs while the finished shots come back
+            flying = len(fin) < len(running)
+            if flying:
+                self.launch()
+            for slot in fin:
                 j = running.pop(slot)
                 results[j] = self.collect(slot, jobs[j])
         return results, {"device_ms": dev_ms, "counted_points": pts, "launches": launches,

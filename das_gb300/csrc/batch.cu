@@ -777,14 +777,16 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
     HostShot& h = b->hs[slot];
     W2D_CHECK_ARG(h.finished, "shot not finished");
     W2D_CHECK_ARG(h.mode == 0, "a modelling job: fetch its gather with w2d_batch_fetch_traces");
+    // on the admission stream: a finished shot's results are complete (w2d_batch_wait
+    // synchronised the replay stream), and the next replay may already be running
     const size_t hp = (size_t)h.nx * 4, dp = (size_t)h.ldx * 4;
     if (image_out)
         W2D_CUDA_TRY(cudaMemcpy2DAsync(image_out, hp, h.image, dp, hp, h.nz,
-                                       cudaMemcpyDeviceToHost, b->st));
+                                       cudaMemcpyDeviceToHost, b->st_up));
     if (illum_out)
         W2D_CUDA_TRY(cudaMemcpy2DAsync(illum_out, hp, h.illum, dp, hp, h.nz,
-                                       cudaMemcpyDeviceToHost, b->st));
-    W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
+                                       cudaMemcpyDeviceToHost, b->st_up));
+    W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
     arena_free(b, h.off, h.bytes);
     h = HostShot();
     return W2D_OK;
@@ -798,8 +800,8 @@ int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out)
     W2D_CHECK_ARG(h.mode == 1, "a migration job: fetch its image with w2d_batch_fetch");
     if (traces_out && h.n_rec > 0)
         W2D_CUDA_TRY(cudaMemcpyAsync(traces_out, h.traces, (size_t)h.nt * h.n_rec * 4,
-                                     cudaMemcpyDeviceToHost, b->st));
-    W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
+                                     cudaMemcpyDeviceToHost, b->st_up));
+    W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
     arena_free(b, h.off, h.bytes);
     h = HostShot();
     return W2D_OK;

@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-constexpr int EL_ADJ_WARPS = 4, EL_ADJ_RPW = 2;  // default tile: 128 x 8
+constexpr int EL_ADJ_WARPS = 4, EL_ADJ_RPW = 1;  // default tile: 128 x 4
 
 inline bool el_adj_tile_supported(int warps, int rpw)
 {

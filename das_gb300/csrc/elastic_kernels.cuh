@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-constexpr int EL_WARPS = 4, EL_RPW = 4;  // default tile: 4 warps x 4 rows (128 x 16)
+constexpr int EL_WARPS = 4, EL_RPW = 2;  // default tile: 4 warps x 2 rows (128 x 8)
 
 // Tile shapes the step kernels are built for (warps per CTA x rows per warp).
 inline bool el_tile_supported(int warps, int rpw)

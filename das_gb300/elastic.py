@@ -49,7 +49,7 @@ class ElasticSolver2D:
     def last_ms(self) -> float:
         return float(self._lib.w2d_elastic_last_ms(self._h))
 
-    def set_tiles(self, step=(4, 4), adjoint=(4, 2)):
+    def set_tiles(self, step=(4, 2), adjoint=(4, 1)):
         """Tile shapes (warps, rows per warp) of the step kernels and the tiled adjoint
         passes; applies from the next forward call; results do not depend on them."""
         _lib.check(self._lib.w2d_elastic_set_tiles(self._h, int(step[0]), int(step[1]),

@@ -116,6 +116,7 @@ class RTMServer:
                 n_shots += len(res)
                 remaining[job_id] = 0
 
+        flying = False  # a replay launched and not yet waited for
         while i < len(trace) or queue or running or (ex is not None and ex.pending()):
             intake()
             admit()
@@ -134,7 +135,8 @@ class RTMServer:
                         dev_clock = max(dev_clock, trace[i].arrival)
                 continue
             max_active = max(max_active, len(running))
-            eng.launch()
+            if not flying:
+                eng.launch()
             if realtime:  # requests arriving during the replay upload while it runs
                 intake()
                 admit()
@@ -142,7 +144,13 @@ class RTMServer:
             busy_ms += eng.last_ms
             pts += eng.last_points
             dev_clock += eng.last_ms / 1e3
-            for slot in [s for s in running if eng.finished(s)]:
+            fin = [s for s in running if eng.finished(s)]
+            # the next replay (the shots still running and those admitted meanwhile)
+            # runs while the finished shots come back
+            flying = len(fin) < len(running)
+            if flying:
+                eng.launch()
+            for slot in fin:
                 req, k = running.pop(slot)
                 sh = req.shots[k]
                 responses[req.job_id].results[k] = eng.fetch(slot, sh.nz, sh.nx)

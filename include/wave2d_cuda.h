@@ -216,7 +216,7 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
  * The two agree to float32 rounding (contraction differs); both are exact adjoints. */
 int w2d_elastic_set_adjoint(w2d_elastic* e, int form);
 /* Tile shapes (warps per CTA x rows per warp, 128 columns wide) of the step kernels
- * (4x4 default, 4x2, 8x2, 8x1) and of the tiled adjoint passes (4x2 default, 4x1,
+ * (4x2 default, 4x4, 8x2, 8x1) and of the tiled adjoint passes (4x1 default, 4x2,
  * 8x1); applies from the next forward call.  Results do not depend on the tiles. */
 int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp,
                           int adjoint_warps, int adjoint_rows_per_warp);
@@ -279,7 +279,8 @@ int w2d_batch_launch(w2d_batch* b);
 int w2d_batch_wait(w2d_batch* b, int* n_finished);
 /* 1 finished, 0 running, -1 unused slot. */
 int w2d_batch_is_finished(w2d_batch* b, int slot);
-/* Copy a finished shot's image and illumination (nz, nx) out and free its memory. */
+/* Copy a finished shot's image and illumination (nz, nx) out and free its memory;
+ * runs beside a replay in flight (launch the next replay first, then fetch). */
 int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out);
 int w2d_batch_cancel(w2d_batch* b, int slot);
 /* Active shots, device ms / counted point-updates / launches of the last step call. */

@@ -159,13 +159,13 @@ def test_tile_shapes_do_not_change_results():
     R = torch.tensor(np.random.default_rng(4).standard_normal((len(w), len(rix))).astype(np.float32),
                      device="cuda")
     out = {}
-    for step, adj in [((4, 4), (4, 2)), ((4, 2), (4, 1)), ((8, 2), (8, 1)), ((8, 1), (4, 2))]:
+    for step, adj in [((4, 2), (4, 1)), ((4, 4), (4, 2)), ((8, 2), (8, 1)), ((8, 1), (4, 2))]:
         solver.set_tiles(step, adj)
         v = torch.tensor(vs, device="cuda", requires_grad=True)
         d = elastic_traces(v, solver, w, 20, 3, rix, 2)
         (d * R).sum().backward()
         out[(step, adj)] = (d.detach().cpu().numpy(), v.grad.cpu().numpy().astype(np.float64))
-    d0, g0 = out[((4, 4), (4, 2))]
+    d0, g0 = out[((4, 2), (4, 1))]
     for k, (d, g) in out.items():
         np.testing.assert_array_equal(d, d0)
         assert np.linalg.norm(g - g0) <= 1e-6 * np.linalg.norm(g0), k
