@@ -189,22 +189,6 @@ static __global__ void el_adj_k4(ElGeom g, ElParams p, ElStrides sd, ElState a, 
     a.sxz[c] = sxz;
 }
 
-// Vertical-strain receivers of u_{n+1} (the source term is added by the step's
-// velocity phase, elastic_kernels.cuh).
-
-// One row of traces per shot (blockIdx.y): vz of shot s at + s * state_stride, its
-// row at out + s * out_stride.
-static __global__ void el_sample_kernel(ElGeom g, const float* vz, size_t state_stride,
-                                        const int* rec_ix, int n_rec, int rec_iz, float* out,
-                                        size_t out_stride)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_rec) return;
-    vz += blockIdx.y * state_stride;
-    out += blockIdx.y * out_stride;
-    out[k] = d_bwd_z(vz, rec_ix[k], rec_iz, g.nx, g.nz, g.ldx) * g.rdz;
-}
-
 // Adjoint of the sampling: adj_vz += Dz-^T (residual) at each receiver, i.e. on
 // rows rec_iz (+c1), rec_iz-1 (-c1), rec_iz+1 (+c2), rec_iz-2 (-c2), cells of M only.
 // One thread per column; receivers sharing a column (CSR rec_ptr / rec_list, in

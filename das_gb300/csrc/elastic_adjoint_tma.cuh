@@ -54,6 +54,17 @@ __device__ __forceinline__ void st4(float* p, const float v[4])
     *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
+// Receiver residuals pass A adds to the adjoint vz before K2 (the adjoint of the
+// vertical-strain sampling, as el_adj_receivers): row n of the residual traces, shot s
+// at + s * resid_stride; receivers by column (CSR ptr / list).  resid null: none.
+struct ElAdjRecv {
+    const float* resid;
+    size_t resid_stride;
+    const int* ptr;
+    const int* list;
+    int rec_iz;
+};
+
 struct ElAdjMaps {
     CUtensorMap tmp;     // the t / r planes (5 per shot)
     CUtensorMap f_next;  // u_{n+1}
@@ -65,7 +76,7 @@ template <int WARPS, int RPW>
 __global__ void __launch_bounds__(WARPS * 32)
     el_adj_a(const __grid_constant__ ElAdjMaps maps, const ElGeom g, const ElParams p,
              const ElStrides sd, ElState a, ElState r, float* g_lam, float* g_mu, float* g_bx,
-             float* g_bz, unsigned* err)
+             float* g_bz, const ElAdjRecv rv, unsigned* err)
 {
     using T = ElAdjTile<WARPS, RPW>;
     extern __shared__ __align__(128) float smem[];
@@ -112,6 +123,29 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* bzp = p.bz + po;
     const int zr0 = z0 + warp * RPW;
     const int sr0 = zr0 - (z0 - 2);
+    if (rv.resid && col_ok && zr0 + RPW > rv.rec_iz - 2 && zr0 <= rv.rec_iz + 1) {
+        // the receivers' residuals on the four rows of their strain stencil (each cell's
+        // contributions in receiver order), added to this thread's own adjoint vz cells
+        // before the rows below read them
+        const float c1 = 9.0f / 8.0f, c2 = -1.0f / 24.0f;
+        const float* res = rv.resid + (size_t)sh * rv.resid_stride;
+        for (int rr = 0; rr < RPW; ++rr) {
+            const int iz = zr0 + rr, dzr = iz - rv.rec_iz;
+            if (dzr < -2 || dzr > 1 || iz >= g.nz) continue;
+            const float cf = dzr == 0 ? c1 : (dzr == -1 ? -c1 : (dzr == 1 ? c2 : -c2));
+            for (int j = 0; j < 4; ++j) {
+                const int ix = ixb + j;
+                if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) continue;
+                const int k0 = __ldg(rv.ptr + ix), k1 = __ldg(rv.ptr + ix + 1);
+                if (k0 == k1) continue;
+                float* cell = a.vz + (size_t)iz * g.ldx + ix;
+                float v = *cell;
+                for (int k = k0; k < k1; ++k)
+                    v = fadd(v, fmul(cf, fmul(__ldg(res + __ldg(rv.list + k)), g.rdz)));
+                *cell = v;
+            }
+        }
+    }
     // Two phases per row (K2, then K3) so that only one phase's operands are live.
 #pragma unroll 1
     for (int rr = 0; rr < RPW; ++rr) {
@@ -357,8 +391,8 @@ inline bool el_adj_tile_supported(int warps, int rpw)
 template <int WARPS, int RPW>
 cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                               const ElStrides& sd, const ElState& a, const ElState& r, float* glam,
-                              float* gmu, float* gbx, float* gbz, unsigned* err, int n_shots,
-                              cudaStream_t st)
+                              float* gmu, float* gbx, float* gbz, const ElAdjRecv& rv,
+                              unsigned* err, int n_shots, cudaStream_t st)
 {
     using T = ElAdjTile<WARPS, RPW>;
     const int bytes = 8 * T::BOX * 4 + 128;
@@ -371,7 +405,7 @@ cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
     el_adj_a<WARPS, RPW><<<grid, WARPS * 32, bytes, st>>>(m, g, p, sd, a, r, glam, gmu, gbx, gbz,
-                                                          err);
+                                                          rv, err);
     return cudaGetLastError();
 }
 
@@ -397,16 +431,20 @@ cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
 // Pass A / pass B on tiles of `warps` x `rpw` rows (maps with box height warps*rpw + 4).
 inline cudaError_t launch_el_adj_a(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                                    const ElStrides& sd, const ElState& a, const ElState& r,
-                                   float* glam, float* gmu, float* gbx, float* gbz, unsigned* err,
-                                   int n_shots, cudaStream_t st, int warps = EL_ADJ_WARPS,
+                                   float* glam, float* gmu, float* gbx, float* gbz,
+                                   const ElAdjRecv& rv, unsigned* err, int n_shots,
+                                   cudaStream_t st, int warps = EL_ADJ_WARPS,
                                    int rpw = EL_ADJ_RPW)
 {
     if (warps == 4 && rpw == 2)
-        return launch_el_adj_a_t<4, 2>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+        return launch_el_adj_a_t<4, 2>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
+                                       st);
     if (warps == 4 && rpw == 1)
-        return launch_el_adj_a_t<4, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+        return launch_el_adj_a_t<4, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
+                                       st);
     if (warps == 8 && rpw == 1)
-        return launch_el_adj_a_t<8, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, err, n_shots, st);
+        return launch_el_adj_a_t<8, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
+                                       st);
     return cudaErrorInvalidValue;
 }
 

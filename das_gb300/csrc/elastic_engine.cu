@@ -124,7 +124,7 @@ ElStrides estrides(w2d_elastic* e)
 // Step n of every shot from the states at src to the states at dst (same pointer:
 // in place), the source term w[n] * dt added to vz at each shot's source first.
 int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, const float* src,
-             float* dst, int n)
+             float* dst, int n, float* trace_row = nullptr)
 {
     ElMaps m;
     m.src = msrc;
@@ -143,6 +143,13 @@ int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, c
     st.nt = e->nt;
     st.n = n;
     st.err = e->err;
+    if (trace_row) {  // receivers sampled by the stress phase
+        st.trace = trace_row;
+        st.rec_ptr = e->rec_ptr;
+        st.rec_list = e->rec_list;
+        st.rec_iz = e->rec_iz;
+        st.trace_stride = (size_t)e->nt * e->n_rec;
+    }
     W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st, e->S, e->map_fwd_warps,
                                      e->map_fwd_rpw));
     return W2D_OK;
@@ -332,16 +339,13 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
     }
     W2D_CUDA_TRY(cudaMemsetAsync(e->state, 0, (size_t)S * SS * 4, e->st));
     W2D_CUDA_TRY(cudaEventRecord(e->e0, e->st));
-    const ElGeom g = egeom(e);
-    const dim3 sgrid((n_rec + 127) / 128, S);
     for (int n = 0; n < nt; ++n) {
         if (n % e->seg_len == 0)
             W2D_CUDA_TRY(cudaMemcpyAsync(e->ckpt + (size_t)(n / e->seg_len) * S * SS, e->state,
                                          (size_t)S * SS * 4, cudaMemcpyDeviceToDevice, e->st));
-        if ((rc = fwd_step(e, e->map_state, e->map_state, e->state, e->state, n))) return rc;
-        el_sample_kernel<<<sgrid, 128, 0, e->st>>>(g, e->state + P, SS, e->rec, n_rec, rec_iz,
-                                                   e->traces + (size_t)n * n_rec,
-                                                   (size_t)nt * n_rec);
+        if ((rc = fwd_step(e, e->map_state, e->map_state, e->state, e->state, n,
+                           e->traces + (size_t)n * n_rec)))
+            return rc;
     }
     W2D_CUDA_TRY(cudaGetLastError());
     W2D_CUDA_TRY(cudaEventRecord(e->e1, e->st));
@@ -386,9 +390,12 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
     float *glam = e->grad, *gmu = e->grad + P, *gbx = e->grad + 2 * P, *gbz = e->grad + 3 * P;
     dim3 blk(32, 8), grd((e->nx + 31) / 32, (e->nz + 7) / 8, S);
     const dim3 rgrid((e->nx + 127) / 128, S);
-    // adjoint of u_nt: residual of the last trace row
-    el_adj_receivers<<<rgrid, 128, 0, e->st>>>(g, a.vz, SS, e->rec_ptr, e->rec_list, e->rec_iz,
-                                               e->traces + (size_t)(nt - 1) * n_rec, tr_stride);
+    // adjoint of u_nt: residual of the last trace row (the tiled pass A adds each
+    // step's row itself)
+    if (e->adj_form != 1)
+        el_adj_receivers<<<rgrid, 128, 0, e->st>>>(g, a.vz, SS, e->rec_ptr, e->rec_list,
+                                                   e->rec_iz, e->traces + (size_t)(nt - 1) * n_rec,
+                                                   tr_stride);
     // K1 of the last step; every later K1 runs inside the K4 of the step after it
     el_adj_k1<<<grd, blk, 0, e->st>>>(g, prm, sd, a, t);
     for (int sgi = e->n_seg - 1; sgi >= 0; --sgi) {
@@ -410,8 +417,10 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 m.tmp = e->adj_map_tmp;
                 m.f_next = e->adj_seg_maps[n + 1 - a0];
                 m.f_curr = e->adj_seg_maps[n - a0];
-                W2D_CUDA_TRY(launch_el_adj_a(m, g, prm, sd, a, r, glam, gmu, gbx, gbz, e->err, S,
-                                             e->st, e->map_adj_warps, e->map_adj_rpw));
+                const ElAdjRecv rv{e->traces + (size_t)n * n_rec, tr_stride, e->rec_ptr,
+                                   e->rec_list, e->rec_iz};
+                W2D_CUDA_TRY(launch_el_adj_a(m, g, prm, sd, a, r, glam, gmu, gbx, gbz, rv, e->err,
+                                             S, e->st, e->map_adj_warps, e->map_adj_rpw));
                 W2D_CUDA_TRY(launch_el_adj_b(m, g, prm, sd, a, t, n >= 1 ? 1 : 0, e->err, S,
                                              e->st, e->map_adj_warps, e->map_adj_rpw));
             } else {
@@ -420,12 +429,11 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 el_adj_k23<<<grd, blk, 0, e->st>>>(g, prm, sd, a, t, r, f_next, f_curr, glam, gmu,
                                                    gbx, gbz);
                 el_adj_k4<<<grd, blk, 0, e->st>>>(g, prm, sd, a, r, t, n >= 1 ? 1 : 0);
+                if (n >= 1)
+                    el_adj_receivers<<<rgrid, 128, 0, e->st>>>(
+                        g, a.vz, SS, e->rec_ptr, e->rec_list, e->rec_iz,
+                        e->traces + (size_t)(n - 1) * n_rec, tr_stride);
             }
-            if (n >= 1)
-                el_adj_receivers<<<rgrid, 128, 0, e->st>>>(g, a.vz, SS, e->rec_ptr, e->rec_list,
-                                                           e->rec_iz,
-                                                           e->traces + (size_t)(n - 1) * n_rec,
-                                                           tr_stride);
         }
     }
     W2D_CUDA_TRY(cudaGetLastError());

@@ -56,6 +56,14 @@ struct ElStep {
     const float* wav;
     int nt, n;
     unsigned* err;
+    // stress phase: the vertical strain Dz- vz of the new velocities at row rec_iz for
+    // every receiver (receivers by column: CSR rec_ptr / rec_list), into trace[k] of
+    // shot s at + s * trace_stride (null: no sampling)
+    float* trace = nullptr;
+    const int* rec_ptr = nullptr;
+    const int* rec_list = nullptr;
+    int rec_iz = 0;
+    size_t trace_stride = 0;
 };
 
 struct ElMaps {
@@ -374,6 +382,20 @@ __global__ void __launch_bounds__(WARPS * 32)
                     szz_d[off + j] = uzz[j];
                     sxz_d[off + j] = uxz[j];
                 }
+            }
+        }
+        if (s.trace && iz == s.rec_iz && col_ok) {
+            // receivers on this row: the strain the stress update itself uses (ez)
+            float* tr = s.trace + (size_t)sh * s.trace_stride;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int ix = ixb + j;
+                if (ix >= g.nx) continue;
+                const int k0 = __ldg(s.rec_ptr + ix), k1 = __ldg(s.rec_ptr + ix + 1);
+                if (k0 == k1) continue;
+                const float d = fmul(
+                    el_dbwd(el_c(z0w, j), el_c(z1w, j), el_c(z2w, j), el_c(z3w, j)), g.rdz);
+                for (int k = k0; k < k1; ++k) tr[__ldg(s.rec_list + k)] = d;
             }
         }
         x0w = x1w;
