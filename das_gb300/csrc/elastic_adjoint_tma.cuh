@@ -94,6 +94,12 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
+    }
+    // set-up overlaps the previous kernel when launched as a programmatic dependent;
+    // every thread waits before any global access
+    grid_dep_launch();
+    grid_dep_wait();
+    if (tid == 0) {
         mbar_expect_tx(bar, 8u * T::BOX * 4u);
         const int xs = x0 - EL_HX, zs = z0 - 2, pb = 5 * sh;
         tma_load_3d(b_txx, &maps.tmp, xs, zs, pb + EL_SXX, bar);
@@ -292,6 +298,10 @@ __global__ void __launch_bounds__(WARPS * 32)
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_mbar_init();
+    }
+    grid_dep_launch();
+    grid_dep_wait();  // as in pass A
+    if (tid == 0) {
         mbar_expect_tx(bar, 2u * T::BOX * 4u);
         tma_load_3d(b_rx, &maps.tmp, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
         tma_load_3d(b_rz, &maps.tmp, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
@@ -392,7 +402,7 @@ template <int WARPS, int RPW>
 cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                               const ElStrides& sd, const ElState& a, const ElState& r, float* glam,
                               float* gmu, float* gbx, float* gbz, const ElAdjRecv& rv,
-                              unsigned* err, int n_shots, cudaStream_t st)
+                              unsigned* err, int n_shots, cudaStream_t st, int pdl)
 {
     using T = ElAdjTile<WARPS, RPW>;
     const int bytes = 8 * T::BOX * 4 + 128;
@@ -404,15 +414,14 @@ cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
         attr_set = true;
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    el_adj_a<WARPS, RPW><<<grid, WARPS * 32, bytes, st>>>(m, g, p, sd, a, r, glam, gmu, gbx, gbz,
-                                                          rv, err);
-    return cudaGetLastError();
+    return el_launch(el_adj_a<WARPS, RPW>, grid, dim3(WARPS * 32), bytes, st, pdl, m, g, p, sd, a,
+                     r, glam, gmu, gbx, gbz, rv, err);
 }
 
 template <int WARPS, int RPW>
 cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                               const ElStrides& sd, const ElState& a, const ElState& t,
-                              int then_k1, unsigned* err, int n_shots, cudaStream_t st)
+                              int then_k1, unsigned* err, int n_shots, cudaStream_t st, int pdl)
 {
     using T = ElAdjTile<WARPS, RPW>;
     const int bytes = 2 * T::BOX * 4 + 128;
@@ -424,8 +433,8 @@ cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
         attr_set = true;
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    el_adj_b<WARPS, RPW><<<grid, WARPS * 32, bytes, st>>>(m, g, p, sd, a, t, then_k1, err);
-    return cudaGetLastError();
+    return el_launch(el_adj_b<WARPS, RPW>, grid, dim3(WARPS * 32), bytes, st, pdl, m, g, p, sd, a,
+                     t, then_k1, err);
 }
 
 // Pass A / pass B on tiles of `warps` x `rpw` rows (maps with box height warps*rpw + 4).
@@ -434,31 +443,31 @@ inline cudaError_t launch_el_adj_a(const ElAdjMaps& m, const ElGeom& g, const El
                                    float* glam, float* gmu, float* gbx, float* gbz,
                                    const ElAdjRecv& rv, unsigned* err, int n_shots,
                                    cudaStream_t st, int warps = EL_ADJ_WARPS,
-                                   int rpw = EL_ADJ_RPW)
+                                   int rpw = EL_ADJ_RPW, int pdl = 0)
 {
     if (warps == 4 && rpw == 2)
         return launch_el_adj_a_t<4, 2>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
-                                       st);
+                                       st, pdl);
     if (warps == 4 && rpw == 1)
         return launch_el_adj_a_t<4, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
-                                       st);
+                                       st, pdl);
     if (warps == 8 && rpw == 1)
         return launch_el_adj_a_t<8, 1>(m, g, p, sd, a, r, glam, gmu, gbx, gbz, rv, err, n_shots,
-                                       st);
+                                       st, pdl);
     return cudaErrorInvalidValue;
 }
 
 inline cudaError_t launch_el_adj_b(const ElAdjMaps& m, const ElGeom& g, const ElParams& p,
                                    const ElStrides& sd, const ElState& a, const ElState& t,
                                    int then_k1, unsigned* err, int n_shots, cudaStream_t st,
-                                   int warps = EL_ADJ_WARPS, int rpw = EL_ADJ_RPW)
+                                   int warps = EL_ADJ_WARPS, int rpw = EL_ADJ_RPW, int pdl = 0)
 {
     if (warps == 4 && rpw == 2)
-        return launch_el_adj_b_t<4, 2>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+        return launch_el_adj_b_t<4, 2>(m, g, p, sd, a, t, then_k1, err, n_shots, st, pdl);
     if (warps == 4 && rpw == 1)
-        return launch_el_adj_b_t<4, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+        return launch_el_adj_b_t<4, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st, pdl);
     if (warps == 8 && rpw == 1)
-        return launch_el_adj_b_t<8, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st);
+        return launch_el_adj_b_t<8, 1>(m, g, p, sd, a, t, then_k1, err, n_shots, st, pdl);
     return cudaErrorInvalidValue;
 }
 

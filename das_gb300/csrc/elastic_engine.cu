@@ -65,6 +65,10 @@ struct w2d_elastic {
     // the tiles the current maps were made for (a change applies at the next forward)
     int map_fwd_warps = EL_WARPS, map_fwd_rpw = EL_RPW, map_adj_warps = EL_ADJ_WARPS,
         map_adj_rpw = EL_ADJ_RPW;
+    // programmatic dependent launches: on/off, and whether the stream's last operation
+    // is a kernel of the step / tiled-adjoint chain (a launch may depend on it only then)
+    int pdl = 1;
+    bool chain = false;
     CUtensorMap adj_map_tmp;                // the adjoint passes' maps (their own box height)
     std::vector<CUtensorMap> adj_seg_maps;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -151,7 +155,8 @@ int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, c
         st.trace_stride = (size_t)e->nt * e->n_rec;
     }
     W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st, e->S, e->map_fwd_warps,
-                                     e->map_fwd_rpw));
+                                     e->map_fwd_rpw, e->pdl && e->chain));
+    e->chain = true;
     return W2D_OK;
 }
 
@@ -339,14 +344,18 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
     }
     W2D_CUDA_TRY(cudaMemsetAsync(e->state, 0, (size_t)S * SS * 4, e->st));
     W2D_CUDA_TRY(cudaEventRecord(e->e0, e->st));
+    e->chain = false;
     for (int n = 0; n < nt; ++n) {
-        if (n % e->seg_len == 0)
+        if (n % e->seg_len == 0) {
             W2D_CUDA_TRY(cudaMemcpyAsync(e->ckpt + (size_t)(n / e->seg_len) * S * SS, e->state,
                                          (size_t)S * SS * 4, cudaMemcpyDeviceToDevice, e->st));
+            e->chain = false;
+        }
         if ((rc = fwd_step(e, e->map_state, e->map_state, e->state, e->state, n,
                            e->traces + (size_t)n * n_rec)))
             return rc;
     }
+    e->chain = false;
     W2D_CUDA_TRY(cudaGetLastError());
     W2D_CUDA_TRY(cudaEventRecord(e->e1, e->st));
     W2D_CUDA_TRY(cudaMemcpyAsync(traces_dev, e->traces, (size_t)S * nt * n_rec * 4,
@@ -403,6 +412,7 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
         // recompute u_a0 .. u_b0 into the segment slots
         W2D_CUDA_TRY(cudaMemcpyAsync(e->slot(0), e->ckpt + (size_t)sgi * S * SS, (size_t)S * SS * 4,
                                      cudaMemcpyDeviceToDevice, e->st));
+        e->chain = false;
         // out of place: slot n - a0 keeps u_n (without the w[n] source term)
         for (int n = a0; n < b0; ++n) {
             const int i = n - a0;
@@ -420,10 +430,13 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 const ElAdjRecv rv{e->traces + (size_t)n * n_rec, tr_stride, e->rec_ptr,
                                    e->rec_list, e->rec_iz};
                 W2D_CUDA_TRY(launch_el_adj_a(m, g, prm, sd, a, r, glam, gmu, gbx, gbz, rv, e->err,
-                                             S, e->st, e->map_adj_warps, e->map_adj_rpw));
+                                             S, e->st, e->map_adj_warps, e->map_adj_rpw,
+                                             e->pdl && e->chain));
                 W2D_CUDA_TRY(launch_el_adj_b(m, g, prm, sd, a, t, n >= 1 ? 1 : 0, e->err, S,
-                                             e->st, e->map_adj_warps, e->map_adj_rpw));
+                                             e->st, e->map_adj_warps, e->map_adj_rpw, e->pdl));
+                e->chain = true;
             } else {
+                e->chain = false;
                 ElState f_next = e->S0(e->slot(n + 1 - a0));  // u_{n+1}
                 ElState f_curr = e->S0(e->slot(n - a0));      // u_n
                 el_adj_k23<<<grd, blk, 0, e->st>>>(g, prm, sd, a, t, r, f_next, f_curr, glam, gmu,
@@ -436,6 +449,7 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
             }
         }
     }
+    e->chain = false;
     W2D_CUDA_TRY(cudaGetLastError());
     W2D_CUDA_TRY(cudaEventRecord(e->e1, e->st));
     float* outs[4] = {g_lam, g_mu, g_bx, g_bz};
@@ -466,6 +480,13 @@ int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
 {
     W2D_CHECK_ARG(e && (form == 0 || form == 1), "form must be 0 (per-cell) or 1 (tiled)");
     e->adj_form = form;
+    return W2D_OK;
+}
+
+int w2d_elastic_set_pdl(w2d_elastic* e, int on)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    e->pdl = on ? 1 : 0;
     return W2D_OK;
 }
 

@@ -29,6 +29,8 @@
 // before the update (the modelling source of the elastic engine).
 #pragma once
 
+#include <utility>
+
 #include "w2d_common.cuh"
 
 namespace w2d {
@@ -173,6 +175,12 @@ __global__ void __launch_bounds__(WARPS * 32)
         prefetch_tensormap(&maps.src);
         mbar_init(bar, 1);
         fence_mbar_init();
+    }
+    // the set-up above overlaps the previous kernel's tail when launched as a
+    // programmatic dependent; every thread waits before any global access
+    grid_dep_launch();
+    grid_dep_wait();
+    if (tid == 0) {
         mbar_expect_tx(bar, 3u * T::BOX * 4u);
         tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXX, bar);
         tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXZ, bar);
@@ -274,6 +282,10 @@ __global__ void __launch_bounds__(WARPS * 32)
         prefetch_tensormap(&maps.dst);
         mbar_init(bar, 1);
         fence_mbar_init();
+    }
+    grid_dep_launch();
+    grid_dep_wait();  // as in the velocity phase
+    if (tid == 0) {
         mbar_expect_tx(bar, 2u * T::BOX * 4u);
         tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
         tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
@@ -423,9 +435,28 @@ inline int make_el_state_map(CUtensorMap* m, const float* base, int nx, int nz, 
     return make_tensor_map_3d(m, base, nx, nz, 5 * n_shots, ldx, plane, EL_SW, tz + 4);
 }
 
+// One launch with an optional programmatic-dependent attribute (the kernel runs its
+// set-up while the previous kernel of the stream finishes, then waits for it).
+template <typename... KArgs, typename... Args>
+inline cudaError_t el_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                             cudaStream_t st, int pdl, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <int WARPS, int RPW>
 cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElStep& s,
-                                  cudaStream_t st, int n_shots)
+                                  cudaStream_t st, int n_shots, int pdl)
 {
     using T = ElTile<WARPS, RPW>;
     const int vbytes = 3 * T::BOX * 4 + 128, sbytes = 2 * T::BOX * 4 + 128;
@@ -440,24 +471,29 @@ cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElS
         attr_set = true;
     }
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    elastic_velocity_kernel<WARPS, RPW><<<grid, WARPS * 32, vbytes, st>>>(maps, g, s);
+    cudaError_t e = el_launch(elastic_velocity_kernel<WARPS, RPW>, grid, dim3(WARPS * 32),
+                              vbytes, st, pdl, maps, g, s);
+    if (e != cudaSuccess) return e;
     ElStep s2 = s;
     s2.src_pos = nullptr;
-    elastic_stress_kernel<WARPS, RPW><<<grid, WARPS * 32, sbytes, st>>>(maps, g, s2);
-    return cudaGetLastError();
+    // the stress phase always follows the velocity kernel directly
+    return el_launch(elastic_stress_kernel<WARPS, RPW>, grid, dim3(WARPS * 32), sbytes, st, 1,
+                     maps, g, s2);
 }
 
 // Velocity then stress phase of one step of n_shots shots (src -> dst; src == dst
 // updates in place), on tiles of `warps` x `rpw` rows; the maps' box height must be
-// warps * rpw + 4.
+// warps * rpw + 4.  pdl: the velocity kernel is a programmatic dependent of the
+// stream's previous operation, which must then be one of this file's or the tiled
+// adjoint's kernels (each waits for its predecessor before any global access).
 inline cudaError_t launch_elastic_step(const ElGeom& g, const ElMaps& maps, const ElStep& s,
                                        cudaStream_t st, int n_shots = 1, int warps = EL_WARPS,
-                                       int rpw = EL_RPW)
+                                       int rpw = EL_RPW, int pdl = 0)
 {
-    if (warps == 4 && rpw == 4) return launch_elastic_step_t<4, 4>(g, maps, s, st, n_shots);
-    if (warps == 4 && rpw == 2) return launch_elastic_step_t<4, 2>(g, maps, s, st, n_shots);
-    if (warps == 8 && rpw == 2) return launch_elastic_step_t<8, 2>(g, maps, s, st, n_shots);
-    if (warps == 8 && rpw == 1) return launch_elastic_step_t<8, 1>(g, maps, s, st, n_shots);
+    if (warps == 4 && rpw == 4) return launch_elastic_step_t<4, 4>(g, maps, s, st, n_shots, pdl);
+    if (warps == 4 && rpw == 2) return launch_elastic_step_t<4, 2>(g, maps, s, st, n_shots, pdl);
+    if (warps == 8 && rpw == 2) return launch_elastic_step_t<8, 2>(g, maps, s, st, n_shots, pdl);
+    if (warps == 8 && rpw == 1) return launch_elastic_step_t<8, 1>(g, maps, s, st, n_shots, pdl);
     return cudaErrorInvalidValue;
 }
 

@@ -55,6 +55,11 @@ class ElasticSolver2D:
         _lib.check(self._lib.w2d_elastic_set_tiles(self._h, int(step[0]), int(step[1]),
                                                    int(adjoint[0]), int(adjoint[1])))
 
+    def set_pdl(self, on: bool = True):
+        """Programmatic dependent launches between consecutive step and tiled-adjoint
+        kernels (on by default); results are identical either way."""
+        _lib.check(self._lib.w2d_elastic_set_pdl(self._h, 1 if on else 0))
+
     def set_adjoint(self, form: str = "tiled"):
         """How the adjoint passes run: "tiled" (TMA-tiled passes, the default) or
         "cells" (one thread per cell); both are exact adjoints of the step and agree

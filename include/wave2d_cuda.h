@@ -220,6 +220,10 @@ int w2d_elastic_set_adjoint(w2d_elastic* e, int form);
  * 8x1); applies from the next forward call.  Results do not depend on the tiles. */
 int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp,
                           int adjoint_warps, int adjoint_rows_per_warp);
+/* Programmatic dependent launches between consecutive step / tiled-adjoint kernels
+ * (on by default; each kernel's set-up overlaps its predecessor's tail, and it waits
+ * for the predecessor before any global access).  Results are identical either way. */
+int w2d_elastic_set_pdl(w2d_elastic* e, int on);
 /* Device bytes one shot of a batch holds (checkpoints, one recomputed segment, fields). */
 unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 

@@ -171,3 +171,25 @@ def test_tile_shapes_do_not_change_results():
         assert np.linalg.norm(g - g0) <= 1e-6 * np.linalg.norm(g0), k
     with pytest.raises(Exception):
         solver.set_tiles((3, 3), (4, 2))
+
+
+def test_programmatic_dependent_launch_does_not_change_results():
+    """Step and tiled-adjoint kernels chained as programmatic dependents (default) and
+    launched plainly: traces and gradients bit-identical, over several checkpoint
+    segments (the copies between segments break the chain)."""
+    from das_gb300.elastic import elastic_traces
+    torch, solver, grid, w, rix = _setup()
+    vs, _ = _model()
+    R = torch.tensor(np.random.default_rng(5).standard_normal((len(w), len(rix))).astype(np.float32),
+                     device="cuda")
+    out = []
+    for on in (True, False):
+        solver.set_pdl(on)
+        v = torch.tensor(np.stack([vs, vs * 1.03]).astype(np.float32), device="cuda",
+                         requires_grad=True)
+        d = elastic_traces(v, solver, np.stack([w, w]), [20, 50], [3, 4], rix, 2)
+        (d * torch.stack([R, R])).sum().backward()
+        out.append((d.detach().cpu().numpy(), v.grad.cpu().numpy()))
+    solver.set_pdl(True)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
