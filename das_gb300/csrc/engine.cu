@@ -10,7 +10,7 @@
 #include <mutex>
 #include <vector>
 
-#include "acoustic_kernels.cuh"
+#include "acoustic_step2.cuh"
 #include "adjoint_kernels.cuh"
 #include "small_kernels.cuh"
 #include "w2d_common.cuh"
@@ -119,16 +119,30 @@ struct w2d_engine {
     DevBuf<float> sponge_lut, sponge_arr;
     bool use_lut = false, use_arr = false;
 
-    DevBuf<float> waves;  // 6 planes: forward triple then backward triple
-    // TMA descriptors for the current tile height: each wave plane as p_curr (halo
-    // box) and as p_prev, each v^2 dt^2 slot, and the per-cell sponge
-    CUtensorMap map_curr[6], map_prev[6], map_vel[2], map_sponge;
+    // 10 physical wave planes: the forward pass's three logical planes (roles by
+    // step, the reference's rotation) plus two spares, the same for the backward pass.
+    // A two-step launch writes its results into the spares and renames: perm maps the
+    // six logical planes (0..2 forward, 3..5 backward) to physical ones.
+    DevBuf<float> waves;
+    int perm[6] = {0, 1, 2, 5, 6, 7};
+    int spare[2][2] = {{3, 4}, {8, 9}};
+    // two time steps per launch where the loop allows (grid launch mode): 0 off (the
+    // default: measured slower than one step per launch on the sponge-framed production
+    // grids), else the tile's rows per warp (2..4); map2_rpw: the shape the two-step
+    // maps were made for
+    int two_step = 0, map2_rpw = -1;
+    // TMA descriptors per physical plane for the current tile height: each wave plane
+    // as p_curr (halo box) and as p_prev, each v^2 dt^2 slot, and the per-cell sponge;
+    // and the two-step kernel's boxes
+    CUtensorMap map_curr[10], map_prev[10], map_vel[2], map_sponge;
+    CUtensorMap map2_curr[10], map2_prev[10], map2_vel[2], map2_sponge;
     int tm_tz = -1;
     DevBuf<float> v2dt2;  // 2 planes (slot 0 forward model, slot 1 backward model)
     bool vel_set[2] = {false, false};
     DevBuf<float> staging;  // one plane, pitched upload area
 
     DevBuf<int> shot;  // {src_ix, src_iz, rec_iz}
+    int h_shot[3] = {-1, -1, -1};  // host copy of the same
     DevBuf<int> rec_ptr, rec_list;
     DevBuf<float> wavelet, data, rec_out;
     DevBuf<float> snaps, ckpt;
@@ -151,7 +165,10 @@ struct w2d_engine {
 
     struct w2d_fwi_state* fwi = nullptr;  // differentiable-path state (checkpoints, gradient)
 
-    float* wave(int i) { return waves.p + (size_t)i * plane; }
+    float* wave(int i) { return waves.p + (size_t)perm[i] * plane; }  // logical plane i
+    float* phys(int k) { return waves.p + (size_t)k * plane; }
+    const CUtensorMap& mcurr(int i) const { return map_curr[perm[i]]; }
+    const CUtensorMap& mprev(int i) const { return map_prev[perm[i]]; }
 };
 
 namespace {
@@ -170,15 +187,40 @@ int download_field(w2d_engine* e, float* host, const float* src_pitched)
     return W2D_OK;
 }
 
+// The two-step kernel's maps for the current rows-per-warp setting.
+int ensure_step2_maps(w2d_engine* e)
+{
+    int rc;
+    const int rpw = e->two_step ? e->two_step : AC2_R2;
+    if (e->map2_rpw == rpw) return W2D_OK;
+    const int cr = ac2_curr_rows(rpw), rr = ac2_ring_rows(rpw);
+    for (int k = 0; k < 10; ++k)
+        if ((rc = make_tensor_map_2d(&e->map2_curr[k], e->phys(k), e->nx, e->nz, e->ldx, AC2_W,
+                                     cr)) ||
+            (rc = make_tensor_map_2d(&e->map2_prev[k], e->phys(k), e->nx, e->nz, e->ldx, AC2_W,
+                                     rr)))
+            return rc;
+    for (int i = 0; i < 2; ++i)
+        if ((rc = make_tensor_map_2d(&e->map2_vel[i], e->v2dt2.p + (size_t)i * e->plane, e->nx,
+                                     e->nz, e->ldx, AC2_W, rr)))
+            return rc;
+    e->map2_sponge = e->map2_vel[0];
+    if (e->use_arr && (rc = make_tensor_map_2d(&e->map2_sponge, e->sponge_arr.p, e->nx, e->nz,
+                                               e->ldx, AC2_W, rr)))
+        return rc;
+    e->map2_rpw = rpw;
+    return W2D_OK;
+}
+
 int ensure_tensor_maps(w2d_engine* e)
 {
     const int tz = e->tile.tz();
-    if (e->tm_tz == tz) return W2D_OK;
+    if (e->tm_tz == tz) return ensure_step2_maps(e);
     int rc;
-    for (int i = 0; i < 6; ++i) {
-        if ((rc = make_tensor_map_2d(&e->map_curr[i], e->wave(i), e->nx, e->nz, e->ldx, AC_SW,
+    for (int k = 0; k < 10; ++k) {
+        if ((rc = make_tensor_map_2d(&e->map_curr[k], e->phys(k), e->nx, e->nz, e->ldx, AC_SW,
                                      tz + 4)) ||
-            (rc = make_tensor_map_2d(&e->map_prev[i], e->wave(i), e->nx, e->nz, e->ldx, AC_TX, tz)))
+            (rc = make_tensor_map_2d(&e->map_prev[k], e->phys(k), e->nx, e->nz, e->ldx, AC_TX, tz)))
             return rc;
     }
     for (int i = 0; i < 2; ++i)
@@ -190,7 +232,7 @@ int ensure_tensor_maps(w2d_engine* e)
                                                e->ldx, AC_TX, tz)))
         return rc;
     e->tm_tz = tz;
-    return W2D_OK;
+    return ensure_step2_maps(e);
 }
 
 int sponge_mode(const w2d_engine* e)
@@ -202,8 +244,8 @@ int sponge_mode(const w2d_engine* e)
 int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcStep& s)
 {
     AcMaps m;
-    m.curr = e->map_curr[curr];
-    m.prev = e->map_prev[prev];
+    m.curr = e->mcurr(curr);
+    m.prev = e->mprev(prev);
     m.vel = e->map_vel[slot];
     m.sponge = e->map_sponge;
     LaunchMode lm;
@@ -217,6 +259,46 @@ int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcS
     W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), lm, m, g, s, e->stream));
     e->chain = true;
     e->last_launches++;
+    return W2D_OK;
+}
+
+// Two steps in one launch: logical planes curr / prev / next of the first step (next:
+// the stale buffer the reference would write); results into the pass's spares, which
+// then take over the logical roles (p_{n+1} -> next, p_{n+2} -> prev).  pass: 0
+// forward, 1 backward.
+int step2(w2d_engine* e, int pass, int curr, int prev, int next, int slot, const AcGeom& g,
+          Ac2Step& p)
+{
+    int* sp = e->spare[pass];
+    Ac2Maps m;
+    m.curr = e->map2_curr[e->perm[curr]];
+    m.prev = e->map2_prev[e->perm[prev]];
+    m.vel = e->map2_vel[slot];
+    m.sponge = e->map2_sponge;
+    m.stale = e->map2_prev[e->perm[next]];
+    p.src_ix = e->h_shot[0];
+    p.src_iz = e->h_shot[1];
+    p.rec_iz = e->h_shot[2];
+    p.out1 = e->phys(sp[0]);
+    p.out2 = e->phys(sp[1]);
+    const int pdl = e->pdl && e->chain;
+    e->chain = false;
+    W2D_CUDA_TRY(launch_acoustic_step2(e->two_step, sponge_mode(e), m, g, p, e->stream, pdl));
+    e->chain = true;
+    e->last_launches++;
+    const int old_next = e->perm[next], old_prev = e->perm[prev];
+    e->perm[next] = sp[0];
+    e->perm[prev] = sp[1];
+    sp[0] = old_next;
+    sp[1] = old_prev;
+    return W2D_OK;
+}
+
+// Zero the three logical planes of a pass (0 forward, 1 backward).
+int zero_pass(w2d_engine* e, int pass)
+{
+    for (int i = 0; i < 3; ++i)
+        W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3 * pass + i), 0, e->plane * 4, e->stream));
     return W2D_OK;
 }
 
@@ -257,6 +339,9 @@ int set_shot(w2d_engine* e, int src_ix, int src_iz, const int* rec_ix, int n_rec
         (rc = e->shot.ensure(4)))
         return rc;
     int sh[4] = {src_ix, src_iz, rec_iz, n_rec};
+    e->h_shot[0] = src_ix;
+    e->h_shot[1] = src_iz;
+    e->h_shot[2] = rec_iz;
     W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_ptr.p, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice,
                                  e->stream));
     W2D_CUDA_TRY(cudaMemcpyAsync(e->rec_list.p, list.data(), list.size() * 4,
@@ -292,21 +377,8 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
 {
     const AcGeom g = geom(e);
     e->chain = false;  // the caller may have enqueued anything before these steps
-    for (int it = it0; it < it1; ++it) {
-        float* prev = e->wave(it % 3);
-        float* curr = e->wave((it + 1) % 3);
-        float* next = e->wave((it + 2) % 3);
-        if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
-            e->chain = false;
-            float* c = o.ckpt + (size_t)(it / o.ckpt_every) * 3 * e->plane;
-            W2D_CUDA_TRY(cudaMemcpyAsync(c, prev, e->plane * 4, cudaMemcpyDeviceToDevice, e->stream));
-            W2D_CUDA_TRY(cudaMemcpyAsync(c + e->plane, curr, e->plane * 4, cudaMemcpyDeviceToDevice,
-                                         e->stream));
-            W2D_CUDA_TRY(cudaMemcpyAsync(c + 2 * e->plane, next, e->plane * 4,
-                                         cudaMemcpyDeviceToDevice, e->stream));
-        }
-        AcStep s = base_step(e);
-        s.p_next = next;
+    auto fwd_opts = [&](AcStep& s, int it) {
+        s = base_step(e);
         s.dt2_inj = dt2inj_f;
         if (it + 1 < o.nt) s.inj_w = e->cur_w + it + 1;
         if (o.rec_out) s.rec_out = o.rec_out + (size_t)it * o.n_rec;
@@ -314,10 +386,37 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
             if (o.snaps) s.snap_out = o.snaps + (size_t)(it / o.interval - o.slot0) * e->plane;
             if (o.illum) s.illum = e->illum.p;
         }
-        int rc = step(e, (it + 1) % 3, it % 3, slot, g, s);
+    };
+    for (int it = it0; it < it1;) {
+        if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
+            e->chain = false;
+            float* c = o.ckpt + (size_t)(it / o.ckpt_every) * 3 * e->plane;
+            W2D_CUDA_TRY(cudaMemcpyAsync(c, e->wave(it % 3), e->plane * 4,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(c + e->plane, e->wave((it + 1) % 3), e->plane * 4,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(c + 2 * e->plane, e->wave((it + 2) % 3), e->plane * 4,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+        }
+        // two steps in one launch unless a checkpoint falls between them
+        const bool pair = e->two_step && !e->persistent && it + 1 < it1 &&
+                          !(o.ckpt && o.ckpt_every > 0 && (it + 1) % o.ckpt_every == 0);
+        int rc;
+        if (pair) {
+            Ac2Step p;
+            memset(&p, 0, sizeof p);
+            fwd_opts(p.s[0], it);
+            fwd_opts(p.s[1], it + 1);
+            rc = step2(e, 0, (it + 1) % 3, it % 3, (it + 2) % 3, slot, g, p);
+            it += 2;
+        } else {
+            AcStep s;
+            fwd_opts(s, it);
+            s.p_next = e->wave((it + 2) % 3);
+            rc = step(e, (it + 1) % 3, it % 3, slot, g, s);
+            it += 1;
+        }
         if (rc) return rc;
-        (void)prev;
-        (void)curr;
     }
     (void)dt2inj;
     return W2D_OK;
@@ -325,7 +424,8 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
 
 int forward_begin(w2d_engine* e, float dt2inj_f)
 {
-    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(0), 0, 3 * e->plane * 4, e->stream));
+    int rc;
+    if ((rc = zero_pass(e, 0))) return rc;
     const AcGeom g = geom(e);
     inject_kernel<<<(e->nx + 255) / 256, 256, 0, e->stream>>>(e->wave(1), g, e->cur_w, nullptr,
                                                               dt2inj_f);
@@ -342,11 +442,8 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
 {
     const AcGeom g = geom(e);
     e->chain = false;  // the caller may have enqueued anything before these steps
-    for (int it = it_hi; it >= it_lo; --it) {
-        const int m = nt - 1 - it;
-        float* next = e->wave(3 + (m + 2) % 3);
-        AcStep s = base_step(e);
-        s.p_next = next;
+    auto bwd_opts = [&](AcStep& s, int it) {
+        s = base_step(e);
         s.dt2_inj = dt2inj_f;
         if (it >= 1 && n_rec > 0) s.inj_data = e->cur_data + (size_t)(it - 1) * n_rec;
         if (snaps && it % interval == 0) {
@@ -357,7 +454,24 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
                 s.img_dt = img_dt;
             }
         }
-        int rc = step(e, 3 + (m + 1) % 3, 3 + m % 3, slot, g, s);
+    };
+    for (int it = it_hi; it >= it_lo;) {
+        const int m = nt - 1 - it;
+        int rc;
+        if (e->two_step && !e->persistent && it - 1 >= it_lo) {
+            Ac2Step p;
+            memset(&p, 0, sizeof p);
+            bwd_opts(p.s[0], it);
+            bwd_opts(p.s[1], it - 1);
+            rc = step2(e, 1, 3 + (m + 1) % 3, 3 + m % 3, 3 + (m + 2) % 3, slot, g, p);
+            it -= 2;
+        } else {
+            AcStep s;
+            bwd_opts(s, it);
+            s.p_next = e->wave(3 + (m + 2) % 3);
+            rc = step(e, 3 + (m + 1) % 3, 3 + m % 3, slot, g, s);
+            it -= 1;
+        }
         if (rc) return rc;
     }
     return W2D_OK;
@@ -365,7 +479,8 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
 
 int backward_begin(w2d_engine* e, int nt, int n_rec, float dt2inj_f)
 {
-    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * e->plane * 4, e->stream));
+    int rc;
+    if ((rc = zero_pass(e, 1))) return rc;
     const AcGeom g = geom(e);
     inject_kernel<<<(e->nx + 255) / 256, 256, 0, e->stream>>>(
         e->wave(4), g, nullptr, e->cur_data + (size_t)(nt - 1) * n_rec, dt2inj_f);
@@ -442,13 +557,13 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
         set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
     }
-    if ((rc = e->waves.ensure(6 * e->plane)) || (rc = e->v2dt2.ensure(2 * e->plane)) ||
+    if ((rc = e->waves.ensure(10 * e->plane)) || (rc = e->v2dt2.ensure(2 * e->plane)) ||
         (rc = e->staging.ensure(e->plane)) || (rc = e->image.ensure(e->plane)) ||
         (rc = e->illum.ensure(e->plane)) || (rc = e->err.ensure(1)) ||
         (rc = e->tile_counter.ensure(1)))
         return fail(rc);
     if (cudaMemset(e->err.p, 0, 4) != cudaSuccess || cudaMemset(e->tile_counter.p, 0, 4) ||
-        cudaMemset(e->waves.p, 0, 6 * e->plane * 4) ||
+        cudaMemset(e->waves.p, 0, 10 * e->plane * 4) ||
         cudaMemset(e->v2dt2.p, 0, 2 * e->plane * 4)) {
         set_error("memset failed");
         return fail(W2D_ECUDA);
@@ -559,6 +674,17 @@ int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
     e->persistent = persistent ? 1 : 0;
     e->pdl = pdl ? 1 : 0;
     return W2D_OK;
+}
+
+int w2d_engine_set_two_step(w2d_engine* e, int rows_per_warp)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CHECK_ARG(rows_per_warp == 0 || rows_per_warp == 1 ||
+                      (rows_per_warp >= 2 && rows_per_warp <= 4),
+                  "rows_per_warp must be 0 (off), 1 (default shape) or 2..4");
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));  // the maps may be in use
+    e->two_step = rows_per_warp == 1 ? AC2_R2 : rows_per_warp;
+    return ensure_step2_maps(e);
 }
 
 int w2d_engine_set_l2_hints(w2d_engine* e, int on)
@@ -686,7 +812,7 @@ int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int n
     if (n_rec > 0) {
         if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
     } else {
-        W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * e->plane * 4, e->stream));
+        if ((rc = zero_pass(e, 1))) return rc;
     }
     if ((rc = run_backward_steps(e, vel_slot, nt, snapshot_interval, n_rec, nt - 1, 0,
                                  n_snaps > 0 ? e->snaps.p : nullptr, 0, n_snaps, img_dt, dt2inj)))
@@ -770,7 +896,7 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
     if (n_rec > 0) {
         if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
     } else {
-        W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * plane_b, e->stream));
+        if ((rc = zero_pass(e, 1))) return rc;
     }
     if (mode == W2D_STORE_ALL) {
         if ((rc = run_backward_steps(e, 1, nt, interval, n_rec, nt - 1, 0, e->snaps.p, 0, n_snaps,
@@ -1208,7 +1334,7 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
     int rc;
     W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, resid_dev, (size_t)nt * n_rec * 4,
                                  cudaMemcpyDeviceToDevice, e->stream));
-    W2D_CUDA_TRY(cudaMemsetAsync(e->wave(3), 0, 3 * plane_b, e->stream));
+    if ((rc = zero_pass(e, 1))) return rc;
     W2D_CUDA_TRY(cudaMemsetAsync(f->grad_c.p, 0, plane_b, e->stream));
     const int hz = e->tile.tz() + 4;
     if ((rc = make_tensor_map_2d(&f->map_c_halo, e->v2dt2.p, e->nx, e->nz, e->ldx, AC_SW, hz)) ||
@@ -1222,8 +1348,8 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
     const AcGeom g = geom(e);
     auto adj = [&](int n, const CUtensorMap& pf) -> int {
         AdjMaps m;
-        m.a1 = e->map_curr[3 + (n + 1) % 3];
-        m.a2 = e->map_prev[3 + (n + 2) % 3];
+        m.a1 = e->mcurr(3 + (n + 1) % 3);
+        m.a2 = e->mprev(3 + (n + 2) % 3);
         m.c = f->map_c_halo;
         m.pf = pf;
         AdjStep s;

@@ -68,6 +68,7 @@ class WaveSolver2D:
         # step launch: one CTA per tile ("grid") or persistent CTAs ("persistent");
         # each optionally a programmatic dependent of the previous step (pdl)
         self.launch = ("grid", True)
+        self.two_step = False  # two time steps per launch (grid launch mode; off by default)
 
     def _default_sponge(self) -> np.ndarray:
         """The Cerjan sponge of this grid's (n_sponge, sponge_alpha) as built at creation."""
@@ -94,6 +95,9 @@ class WaveSolver2D:
             _lib.check(self._lib.w2d_engine_set_l2_hints(h, 1))
         if self.launch != ("grid", True):
             self._apply_launch(h)
+        if self.two_step is not False:
+            v = 1 if self.two_step is True else int(self.two_step)
+            _lib.check(self._lib.w2d_engine_set_two_step(h, v))
         return h
 
     def _apply_launch(self, h):
@@ -108,6 +112,14 @@ class WaveSolver2D:
         self.launch = (kind, bool(pdl))
         if self._engine is not None:
             self._apply_launch(self._engine)
+
+    def set_two_step(self, on=True) -> None:
+        """Two time steps per launch (True, or an int 2..4: the tile's rows per warp) or
+        one (False, the default: faster on sponge-framed grids).  Results are identical."""
+        self.two_step = on if isinstance(on, bool) else int(on)
+        if self._engine is not None:
+            v = (1 if on else 0) if isinstance(on, bool) else int(on)
+            _lib.check(self._lib.w2d_engine_set_two_step(self._engine, v))
 
     def close(self):
         if getattr(self, "_engine", None) is not None:

@@ -105,6 +105,12 @@ int w2d_engine_set_l2_hints(w2d_engine* e, int on);
  * launches each step as a programmatic dependent of the previous one, so its
  * set-up overlaps the previous step's tail.  Default: persistent 0, pdl 1. */
 int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl);
+/* Two time steps per launch (one-CTA-per-tile mode only): each 128 x (4 *
+ * rows_per_warp) tile evaluates step n on itself plus a 2-cell ring in shared memory,
+ * then step n+1, so every wavefield crosses memory once per two steps; bit-identical
+ * to one step per launch.  Checkpoint boundaries fall back to single steps.
+ * rows_per_warp: 0 off (the default), 1 the default shape (3), 2..4. */
+int w2d_engine_set_two_step(w2d_engine* e, int rows_per_warp);
 
 /* forward_propagate_acoustic, wave_solver.py:128-186.  rec_out: (nt, n_rec);
  * snaps_out: (ceil(nt/interval), nz, nx) or NULL.  Indices already in range. */
