@@ -60,6 +60,8 @@ struct w2d_batch {
     int* d_active = nullptr;
     int* d_prefix = nullptr;
     int* d_nact = nullptr;
+    int2* d_items = nullptr;  // grid form: per CTA {slot, tile} of the active shots
+    size_t items_cap = 0;
     unsigned* d_head = nullptr;
     unsigned* d_err = nullptr;
     std::vector<BShot> h_shots;
@@ -218,8 +220,7 @@ int capture_grid_replay(w2d_batch* b, int steps)
     BatchStepArgs a;
     a.shots = b->d_shots;
     a.maps = b->d_maps;
-    a.active = b->d_active;
-    a.tile_prefix = b->d_prefix;
+    a.items = b->d_items;
     a.n_active = (int)b->active.size();
     a.max_shots = b->max_shots;
     a.err = b->d_err;
@@ -365,7 +366,8 @@ void w2d_batch_destroy(w2d_batch* b)
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->gexec_grid) cudaGraphExecDestroy(b->gexec_grid);
     for (void* p : {(void*)b->arena, (void*)b->d_shots, (void*)b->d_maps, (void*)b->d_active,
-                    (void*)b->d_prefix, (void*)b->d_nact, (void*)b->d_head, (void*)b->d_err})
+                    (void*)b->d_prefix, (void*)b->d_nact, (void*)b->d_head, (void*)b->d_err,
+                    (void*)b->d_items})
         if (p) cudaFree(p);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
@@ -411,6 +413,10 @@ int w2d_batch_set_form(w2d_batch* b, int form)
     W2D_CHECK_ARG(b, "batch is NULL");
     W2D_CHECK_ARG(form == 0 || form == 1, "form must be 0 (queue) or 1 (grid)");
     W2D_CHECK_ARG(!b->in_flight, "change the form between replays only");
+    if (form != b->form) {
+        b->active_dirty = true;  // the grid form's work table is built with the active list
+        b->grid_key = -1;
+    }
     b->form = form;
     return W2D_OK;
 }
@@ -684,6 +690,27 @@ int w2d_batch_launch(w2d_batch* b)
                                      cudaMemcpyHostToDevice, b->st));
         W2D_CUDA_TRY(cudaMemcpyAsync(b->d_nact, &n, 4, cudaMemcpyHostToDevice, b->st));
         b->t_all = prefix[n];
+        if (b->form == 1) {
+            // the grid form's work table: CTA r takes tile r - prefix[i] of active shot i
+            if ((size_t)b->t_all > b->items_cap) {
+                if (b->d_items) {
+                    W2D_CUDA_TRY(cudaStreamSynchronize(b->st));  // the last replay read it
+                    cudaFree(b->d_items);
+                    b->d_items = nullptr;
+                    b->items_cap = 0;
+                }
+                const size_t cap = std::max<size_t>(1024, 2 * (size_t)b->t_all);
+                W2D_CUDA_TRY(cudaMalloc(&b->d_items, cap * sizeof(int2)));
+                b->items_cap = cap;
+                b->grid_key = -1;  // the captured replay holds the old table's address
+            }
+            std::vector<int2> items(b->t_all);
+            for (int i = 0; i < n; ++i)
+                for (int t = 0; t < prefix[i + 1] - prefix[i]; ++t)
+                    items[prefix[i] + t] = make_int2(b->active[i], t);
+            W2D_CUDA_TRY(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2),
+                                         cudaMemcpyHostToDevice, b->st));
+        }
         b->active_dirty = false;
     }
     if (b->form == 1) {

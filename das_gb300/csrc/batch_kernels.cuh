@@ -213,8 +213,7 @@ __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1
 struct BatchStepArgs {
     BShot* shots;
     const BMaps* maps;
-    const int* active;       // indices of active shots
-    const int* tile_prefix;  // prefix sums of their tile counts
+    const int2* items;       // per CTA: {shot slot, tile}, the active shots' tiles in order
     int n_active;
     int max_shots;           // size of the shot table (range check of active entries)
     int j;                   // phase step k0 + j of every active shot
@@ -238,23 +237,21 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_step_kernel(const B
         fence_mbar_init();
     }
     grid_dep_launch();
-    grid_dep_wait();  // shot progress and the active list come from earlier launches
-    const int r = blockIdx.x;
-    int lo = 0, hi = a.n_active - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(a.tile_prefix + mid) <= r) lo = mid;
-        else hi = mid - 1;
-    }
-    const int slot = __ldg(a.active + lo);
-    const int t = r - __ldg(a.tile_prefix + lo);
-    if (slot < 0 || slot >= a.max_shots || t < 0) {  // inconsistent active list: skip, report
+    // The work table and the shots' fixed fields do not change during a replay (they are
+    // written before its first launch, which waits for the stream normally): read them
+    // while the previous launch drains.  The progress k0 changes between chunks.
+    const int2 it = __ldg(a.items + blockIdx.x);
+    const int slot = it.x, t = it.y;
+    if (slot < 0 || slot >= a.max_shots || t < 0) {  // inconsistent work table: skip, report
+        grid_dep_wait();
         if (tid == 0) atomicOr(a.err, ERR_BAD_ITEM);
         return;
     }
     const BShot* sh = a.shots + slot;
+    const int ntiles = sh->ntiles, k_end = sh->k_end;
+    grid_dep_wait();
     const int k = sh->k0 + a.j;
-    if (t >= sh->ntiles || k >= sh->k_end) return;
+    if (t >= ntiles || k >= k_end) return;
     AcStep s;
     int ci, pi, vi;
     batch_phase(sh, k, a.err, s, ci, pi, vi);
