@@ -81,8 +81,40 @@ enum { EL_VX = 0, EL_VZ = 1, EL_SXX = 2, EL_SZZ = 3, EL_SXZ = 4 };
 template <int WARPS, int RPW>
 struct ElTile {
     static constexpr int TZ = WARPS * RPW;
-    static constexpr int BOX = (TZ + 4) * EL_SW;  // floats per box
+    static constexpr int BOX = (TZ + 4) * EL_SW;  // floats per halo box
+    static constexpr int PT = TZ * EL_TX;         // floats per pointwise field of the tile
+    static constexpr int V_FLOATS = 3 * BOX + 5 * PT;  // velocity phase
+    static constexpr int S_FLOATS = 2 * BOX + 6 * PT;  // stress phase
 };
+
+// Each thread stages the float4s of the pointwise fields it will use (its warp's rows,
+// its four columns) into shared memory with asynchronous copies issued at entry, so
+// their latency overlaps the halo boxes' instead of following it.
+template <int WARPS, int RPW>
+__device__ __forceinline__ void el_stage_pointwise(float* pt, const float* const* fields,
+                                                   int n_fields, int zr0, int ixb, int lane,
+                                                   int warp, const ElGeom& g)
+{
+    using T = ElTile<WARPS, RPW>;
+    if (ixb >= g.ldx) return;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+        const int iz = zr0 + r;
+        if (iz >= g.nz) continue;
+        const size_t off = (size_t)iz * g.ldx + ixb;
+        const int lr = warp * RPW + r;
+        for (int f = 0; f < n_fields; ++f)
+            if (fields[f]) cp_async16(&pt[(f * T::TZ + lr) * EL_TX + 4 * lane], fields[f] + off);
+    }
+}
+
+// The float4 a thread staged for field f, row r of its warp.
+template <int WARPS, int RPW>
+__device__ __forceinline__ float4 el_staged(const float* pt, int f, int warp, int r, int lane)
+{
+    using T = ElTile<WARPS, RPW>;
+    return *reinterpret_cast<const float4*>(&pt[(f * T::TZ + warp * RPW + r) * EL_TX + 4 * lane]);
+}
 
 // c1*(a[+s]-a[0]) + c2*(a[+2s]-a[-s])
 __device__ __forceinline__ float el_dfwd(float am1, float a0, float ap1, float ap2)
@@ -168,7 +200,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* bxx = smem;             // sxx box
     float* bxz = smem + T::BOX;    // sxz box
     float* bzz = smem + 2 * T::BOX;  // szz box
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 3 * T::BOX);
+    float* pt = smem + 3 * T::BOX;   // staged vx, vz, bx, bz, sponge
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::V_FLOATS);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
@@ -186,12 +219,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXZ, bar);
         tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SZZ, bar);
     }
-    __syncthreads();
-    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
-    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
-        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
-        return;
-    }
     // every lane takes part in the shuffles; lanes past the row pitch only skip
     // their loads and stores
     const int ixb = x0 + 4 * lane;
@@ -204,6 +231,19 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* vz_d = s.dst + so + (size_t)EL_VZ * s.plane;
     const float* bxp = s.bx + po;
     const float* bzp = s.bz + po;
+    const int zr0 = z0 + warp * RPW;
+    {
+        const float* f[5] = {vx_s, vz_s, bxp, bzp, g.sponge};
+        el_stage_pointwise<WARPS, RPW>(pt, f, 5, zr0, ixb, lane, warp, g);
+    }
+    __syncthreads();
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        cp_async_wait_all();
+        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    cp_async_wait_all();  // this thread's staged fields (read only by this thread)
     int inj_ix = -1, inj_iz = -1;
     float inj = 0.0f;
     if (s.src_pos) {
@@ -211,7 +251,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         inj_iz = __ldg(s.src_pos + 2 * sh + 1);
         inj = fmul(__ldg(s.wav + (size_t)sh * s.nt + s.n), g.dt);
     }
-    const int zr0 = z0 + warp * RPW;
     const int sr = zr0 - (z0 - 2);  // box row of global row zr0
     // z windows: sxz rows z-2..z+1, szz rows z-1..z+2
     float4 xz0 = el_row4(bxz, sr - 2, lane), xz1 = el_row4(bxz, sr - 1, lane),
@@ -228,11 +267,11 @@ __global__ void __launch_bounds__(WARPS * 32)
         el_xrow(bxz, sr + r, lane, exz);
         if (iz < g.nz && col_ok) {
             const size_t off = (size_t)iz * g.ldx + ixb;
-            const float4 vx4 = __ldg(reinterpret_cast<const float4*>(vx_s + off));
-            float4 vz4 = __ldg(reinterpret_cast<const float4*>(vz_s + off));
-            const float4 bx4 = __ldg(reinterpret_cast<const float4*>(bxp + off));
-            const float4 bz4 = __ldg(reinterpret_cast<const float4*>(bzp + off));
-            const float4 sp4 = g.sponge ? __ldg(reinterpret_cast<const float4*>(g.sponge + off))
+            const float4 vx4 = el_staged<WARPS, RPW>(pt, 0, warp, r, lane);
+            float4 vz4 = el_staged<WARPS, RPW>(pt, 1, warp, r, lane);
+            const float4 bx4 = el_staged<WARPS, RPW>(pt, 2, warp, r, lane);
+            const float4 bz4 = el_staged<WARPS, RPW>(pt, 3, warp, r, lane);
+            const float4 sp4 = g.sponge ? el_staged<WARPS, RPW>(pt, 4, warp, r, lane)
                                         : make_float4(1.f, 1.f, 1.f, 1.f);
             float ux[4], uz[4];
 #pragma unroll
@@ -275,7 +314,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     extern __shared__ __align__(128) float smem[];
     float* bvx = smem;
     float* bvz = smem + T::BOX;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::BOX);
+    float* pt = smem + 2 * T::BOX;  // staged lambda, mu, sxx, szz, sxz, sponge
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::S_FLOATS);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
@@ -290,12 +330,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
         tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
     }
-    __syncthreads();
-    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
-    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
-        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
-        return;
-    }
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;  // see the velocity phase
     const bool in_place = s.src == s.dst;
@@ -309,6 +343,18 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* lamp = s.lam + po;
     const float* mup = s.mu + po;
     const int zr0 = z0 + warp * RPW;
+    {
+        const float* f[6] = {lamp, mup, sxx_s, szz_s, sxz_s, g.sponge};
+        el_stage_pointwise<WARPS, RPW>(pt, f, 6, zr0, ixb, lane, warp, g);
+    }
+    __syncthreads();
+    // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        cp_async_wait_all();
+        if (tid == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    cp_async_wait_all();  // this thread's staged fields (read only by this thread)
     const int sr = zr0 - (z0 - 2);
     // z windows: vx rows z-1..z+2, vz rows z-2..z+1
     float4 x0w = el_row4(bvx, sr - 1, lane), x1w = el_row4(bvx, sr, lane),
@@ -325,12 +371,12 @@ __global__ void __launch_bounds__(WARPS * 32)
         el_xrow(bvz, sr + r, lane, evz);
         if (iz < g.nz && col_ok) {
             const size_t off = (size_t)iz * g.ldx + ixb;
-            const float4 lam4 = __ldg(reinterpret_cast<const float4*>(lamp + off));
-            const float4 mu4 = __ldg(reinterpret_cast<const float4*>(mup + off));
-            const float4 sxx4 = __ldg(reinterpret_cast<const float4*>(sxx_s + off));
-            const float4 szz4 = __ldg(reinterpret_cast<const float4*>(szz_s + off));
-            const float4 sxz4 = __ldg(reinterpret_cast<const float4*>(sxz_s + off));
-            const float4 sp4 = g.sponge ? __ldg(reinterpret_cast<const float4*>(g.sponge + off))
+            const float4 lam4 = el_staged<WARPS, RPW>(pt, 0, warp, r, lane);
+            const float4 mu4 = el_staged<WARPS, RPW>(pt, 1, warp, r, lane);
+            const float4 sxx4 = el_staged<WARPS, RPW>(pt, 2, warp, r, lane);
+            const float4 szz4 = el_staged<WARPS, RPW>(pt, 3, warp, r, lane);
+            const float4 sxz4 = el_staged<WARPS, RPW>(pt, 4, warp, r, lane);
+            const float4 sp4 = g.sponge ? el_staged<WARPS, RPW>(pt, 5, warp, r, lane)
                                         : make_float4(1.f, 1.f, 1.f, 1.f);
             float uxx[4], uzz[4], uxz[4];
 #pragma unroll
@@ -459,7 +505,7 @@ cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElS
                                   cudaStream_t st, int n_shots, int pdl)
 {
     using T = ElTile<WARPS, RPW>;
-    const int vbytes = 3 * T::BOX * 4 + 128, sbytes = 2 * T::BOX * 4 + 128;
+    const int vbytes = T::V_FLOATS * 4 + 128, sbytes = T::S_FLOATS * 4 + 128;
     static bool attr_set = false;  // one attribute call per process and shape
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(elastic_velocity_kernel<WARPS, RPW>,
