@@ -22,6 +22,9 @@ template <int WARPS, int RPW>
 struct ElAdjTile {
     static constexpr int TZ = WARPS * RPW;
     static constexpr int BOX = (TZ + 4) * EL_SW;
+    static constexpr int PT = TZ * EL_TX;              // one staged pointwise field
+    static constexpr int A_FLOATS = 8 * BOX + 12 * PT;  // pass A
+    static constexpr int B_FLOATS = 2 * BOX + 6 * PT;   // pass B
 };
 
 // c1*(a[x+1]-a[x]) + c2*(a[x+2]-a[x-1]) of point j from an el_xrow row
@@ -88,7 +91,9 @@ __global__ void __launch_bounds__(WARPS * 32)
     float* b_cxx = smem + 5 * T::BOX;
     float* b_cxz = smem + 6 * T::BOX;
     float* b_czz = smem + 7 * T::BOX;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 8 * T::BOX);
+    // staged: adj vx, vz, sxx, szz, sxz, g_lambda, g_mu, sponge, bx, bz, g_bx, g_bz
+    float* pt = smem + 8 * T::BOX;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::A_FLOATS);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
@@ -111,11 +116,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         tma_load_3d(b_cxz, &maps.f_curr, xs, zs, pb + EL_SXZ, bar);
         tma_load_3d(b_czz, &maps.f_curr, xs, zs, pb + EL_SZZ, bar);
     }
-    __syncthreads();
-    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
-        if (tid == 0) atomicOr(err, ERR_TMA_TIMEOUT);
-        return;
-    }
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;
     const size_t so = (size_t)sh * sd.state, po = (size_t)sh * sd.param, go = (size_t)sh * sd.grad;
@@ -129,10 +129,23 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* bzp = p.bz + po;
     const int zr0 = z0 + warp * RPW;
     const int sr0 = zr0 - (z0 - 2);
+    {
+        const float* f[12] = {a.vx, a.vz, a.sxx, a.szz, a.sxz, g_lam, g_mu,
+                              p.sponge, bxp, bzp, g_bx, g_bz};
+        el_stage_pointwise<WARPS, RPW>(pt, f, 12, zr0, ixb, lane, warp, g);
+    }
+    __syncthreads();
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        cp_async_wait_all();
+        if (tid == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    cp_async_wait_all();  // this thread's staged fields (read and updated only by it)
+    auto staged = [&](int f, int rr) { return el_staged<WARPS, RPW>(pt, f, warp, rr, lane); };
     if (rv.resid && col_ok && zr0 + RPW > rv.rec_iz - 2 && zr0 <= rv.rec_iz + 1) {
         // the receivers' residuals on the four rows of their strain stencil (each cell's
-        // contributions in receiver order), added to this thread's own adjoint vz cells
-        // before the rows below read them
+        // contributions in receiver order), added to this thread's staged adjoint vz
+        // before the rows below read it
         const float c1 = 9.0f / 8.0f, c2 = -1.0f / 24.0f;
         const float* res = rv.resid + (size_t)sh * rv.resid_stride;
         for (int rr = 0; rr < RPW; ++rr) {
@@ -144,7 +157,7 @@ __global__ void __launch_bounds__(WARPS * 32)
                 if (!el_in_m(ix, iz, g.nx, g.nz, g.free_surface)) continue;
                 const int k0 = __ldg(rv.ptr + ix), k1 = __ldg(rv.ptr + ix + 1);
                 if (k0 == k1) continue;
-                float* cell = a.vz + (size_t)iz * g.ldx + ix;
+                float* cell = &pt[(1 * T::TZ + warp * RPW + rr) * EL_TX + 4 * lane + j];
                 float v = *cell;
                 for (int k = k0; k < k1; ++k)
                     v = fadd(v, fmul(cf, fmul(__ldg(res + __ldg(rv.list + k)), g.rdz)));
@@ -185,10 +198,9 @@ __global__ void __launch_bounds__(WARPS * 32)
                 const float4 nvz_m2 = el_row4(b_nvz, sr - 2, lane),
                              nvz_m1 = el_row4(b_nvz, sr - 1, lane),
                              nvz_p1 = el_row4(b_nvz, sr + 1, lane);
-                const float4 avx4 = ld4(a.vx + off), avz4 = ld4(a.vz + off);
-                const float4 qxx4 = ld4(a.sxx + off), qzz4 = ld4(a.szz + off),
-                             qxz4 = ld4(a.sxz + off);
-                const float4 gl4 = ld4(g_lam + off), gm4 = ld4(g_mu + off);
+                const float4 avx4 = staged(0, rr), avz4 = staged(1, rr);
+                const float4 qxx4 = staged(2, rr), qzz4 = staged(3, rr), qxz4 = staged(4, rr);
+                const float4 gl4 = staged(5, rr), gm4 = staged(6, rr);
                 float o_gl[4], o_gm[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -237,9 +249,9 @@ __global__ void __launch_bounds__(WARPS * 32)
                 const float4 czz_m1 = el_row4(b_czz, sr - 1, lane), czz_c = el_row4(b_czz, sr, lane),
                              czz_p1 = el_row4(b_czz, sr + 1, lane),
                              czz_p2 = el_row4(b_czz, sr + 2, lane);
-                const float4 sp4 = p.sponge ? ld4(p.sponge + off) : make_float4(1.f, 1.f, 1.f, 1.f);
-                const float4 bx4 = ld4(bxp + off), bz4 = ld4(bzp + off);
-                const float4 gbx4 = ld4(g_bx + off), gbz4 = ld4(g_bz + off);
+                const float4 sp4 = p.sponge ? staged(7, rr) : make_float4(1.f, 1.f, 1.f, 1.f);
+                const float4 bx4 = staged(8, rr), bz4 = staged(9, rr);
+                const float4 gbx4 = staged(10, rr), gbz4 = staged(11, rr);
                 float o_gbx[4], o_gbz[4], o_rx[4], o_rz[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -292,7 +304,8 @@ __global__ void __launch_bounds__(WARPS * 32)
     extern __shared__ __align__(128) float smem[];
     float* b_rx = smem;
     float* b_rz = smem + T::BOX;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * T::BOX);
+    float* pt = smem + 2 * T::BOX;  // staged adj sxx, szz, sxz, sponge, lambda, mu
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::B_FLOATS);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * EL_TX, z0 = blockIdx.y * T::TZ, sh = blockIdx.z;
     if (tid == 0) {
@@ -306,11 +319,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         tma_load_3d(b_rx, &maps.tmp, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
         tma_load_3d(b_rz, &maps.tmp, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
     }
-    __syncthreads();
-    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
-        if (tid == 0) atomicOr(err, ERR_TMA_TIMEOUT);
-        return;
-    }
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;
     const size_t so = (size_t)sh * sd.state, po = (size_t)sh * sd.param;
@@ -320,6 +328,18 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* mup = p.mu + po;
     const int zr0 = z0 + warp * RPW;
     const int sr0 = zr0 - (z0 - 2);
+    {
+        const float* f[6] = {a.sxx, a.szz, a.sxz, then_k1 ? p.sponge : nullptr,
+                             then_k1 ? lamp : nullptr, then_k1 ? mup : nullptr};
+        el_stage_pointwise<WARPS, RPW>(pt, f, 6, zr0, ixb, lane, warp, g);
+    }
+    __syncthreads();
+    if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
+        cp_async_wait_all();
+        if (tid == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+        return;
+    }
+    cp_async_wait_all();  // this thread's staged fields (read only by it)
 #pragma unroll
     for (int rr = 0; rr < RPW; ++rr) {
         const int iz = zr0 + rr, sr = sr0 + rr;
@@ -332,12 +352,14 @@ __global__ void __launch_bounds__(WARPS * 32)
         const float4 rz_m2 = el_row4(b_rz, sr - 2, lane), rz_m1 = el_row4(b_rz, sr - 1, lane),
                      rz_p1 = el_row4(b_rz, sr + 1, lane);
         const size_t off = (size_t)iz * g.ldx + ixb;
-        const float4 sxx4 = ld4(a.sxx + off), szz4 = ld4(a.szz + off), sxz4 = ld4(a.sxz + off);
+        const float4 sxx4 = el_staged<WARPS, RPW>(pt, 0, warp, rr, lane),
+                     szz4 = el_staged<WARPS, RPW>(pt, 1, warp, rr, lane),
+                     sxz4 = el_staged<WARPS, RPW>(pt, 2, warp, rr, lane);
         float4 sp4 = make_float4(1.f, 1.f, 1.f, 1.f), l4 = sp4, m4 = sp4;
         if (then_k1) {
-            if (p.sponge) sp4 = ld4(p.sponge + off);
-            l4 = ld4(lamp + off);
-            m4 = ld4(mup + off);
+            if (p.sponge) sp4 = el_staged<WARPS, RPW>(pt, 3, warp, rr, lane);
+            l4 = el_staged<WARPS, RPW>(pt, 4, warp, rr, lane);
+            m4 = el_staged<WARPS, RPW>(pt, 5, warp, rr, lane);
         }
         float oxx[4], ozz[4], oxz[4], txx[4], tzz[4], txz[4];
         bool all = true;
@@ -405,7 +427,7 @@ cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
                               unsigned* err, int n_shots, cudaStream_t st, int pdl)
 {
     using T = ElAdjTile<WARPS, RPW>;
-    const int bytes = 8 * T::BOX * 4 + 128;
+    const int bytes = T::A_FLOATS * 4 + 128;
     static bool attr_set = false;  // one attribute call per process and shape
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(el_adj_a<WARPS, RPW>,
@@ -424,7 +446,7 @@ cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
                               int then_k1, unsigned* err, int n_shots, cudaStream_t st, int pdl)
 {
     using T = ElAdjTile<WARPS, RPW>;
-    const int bytes = 2 * T::BOX * 4 + 128;
+    const int bytes = T::B_FLOATS * 4 + 128;
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(el_adj_b<WARPS, RPW>,
