@@ -157,6 +157,11 @@ struct w2d_engine {
     std::vector<DevBuf<float>> st_w, st_d;
     std::vector<int> st_nt, st_nrec;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    // receiver data of a migration uploads on its own stream beside the forward pass
+    // (which does not read it); the backward pass waits for data_ready
+    cudaStream_t up = nullptr;
+    cudaEvent_t up_after = nullptr, data_ready = nullptr;
+    bool data_pending = false;
 
     // stats of the last call
     int last_storage = 0;
@@ -553,7 +558,10 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
         return code;
     };
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
+        cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&e->up, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->up_after, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->data_ready, cudaEventDisableTiming) != cudaSuccess) {
         set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
     }
@@ -651,6 +659,10 @@ void w2d_engine_destroy(w2d_engine* e)
     if (e->t1) cudaEventDestroy(e->t1);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->up) cudaStreamSynchronize(e->up);
+    if (e->up_after) cudaEventDestroy(e->up_after);
+    if (e->data_ready) cudaEventDestroy(e->data_ready);
+    if (e->up) cudaStreamDestroy(e->up);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
 }
@@ -893,6 +905,10 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
     e->last_launches++;
 
     // 2. backward pass in slot 1 with imaging
+    if (e->data_pending) {  // the receiver data uploaded beside the forward pass
+        W2D_CUDA_TRY(cudaStreamWaitEvent(e->stream, e->data_ready, 0));
+        e->data_pending = false;
+    }
     if (n_rec > 0) {
         if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
     } else {
@@ -975,12 +991,24 @@ int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, in
         return rc;
     W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet.p, wavelet, (size_t)nt * 4, cudaMemcpyHostToDevice,
                                  e->stream));
-    if (n_rec > 0)
+    if (n_rec > 0) {
+        // after everything already on the engine stream (an earlier pass may still read
+        // the data buffer), beside the forward pass of this one
+        W2D_CUDA_TRY(cudaEventRecord(e->up_after, e->stream));
+        W2D_CUDA_TRY(cudaStreamWaitEvent(e->up, e->up_after, 0));
         W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, data, (size_t)nt * n_rec * 4,
-                                     cudaMemcpyHostToDevice, e->stream));
+                                     cudaMemcpyHostToDevice, e->up));
+        W2D_CUDA_TRY(cudaEventRecord(e->data_ready, e->up));
+        e->data_pending = true;
+    }
     e->cur_w = e->wavelet.p;
     e->cur_data = e->data.p;
-    return migrate_core(e, nt, n_rec, snapshot_interval, storage, image_out, illum_out);
+    const int rc2 = migrate_core(e, nt, n_rec, snapshot_interval, storage, image_out, illum_out);
+    if (e->data_pending) {  // an early return before the backward pass: settle the copy
+        cudaStreamSynchronize(e->up);
+        e->data_pending = false;
+    }
+    return rc2;
 }
 
 int w2d_shot_stage(w2d_engine* e, int slot, const float* wavelet, int nt, const float* data,
