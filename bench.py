@@ -440,6 +440,26 @@ def _batched_jobs(n, seed, nt_scale=1.0, pinned=False):
     return jobs
 
 
+def cpu_job_rate(job, nt_sample):
+    """The reference's CPU path (oracle port of wave2d.c and its Python loops, all host
+    cores) on one ShotJob truncated to nt_sample steps: (counted Gpts/s, seconds)."""
+    threads = len(os.sched_getaffinity(0))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as o
+    kind = "reference" if o.reference_available() else "port"
+    o.set_backend("reference" if kind == "reference" else "native")
+    o.set_num_threads(threads)
+    g = o.Grid(job.nx, job.nz, job.dx, job.dz, job.dt, job.n_sponge, job.sponge_alpha,
+               job.free_surface_top)
+    n = min(nt_sample, len(job.wavelet))
+    t0 = time.perf_counter()
+    o.migrate_shot(g, job.vel_fwd, job.vel_bwd, job.wavelet[:n], job.source_ix, job.source_iz,
+                   np.ascontiguousarray(job.data[:n]), job.receiver_ix, job.receiver_iz,
+                   job.snapshot_interval, sponge=g.sponge(), native=True)
+    el = time.perf_counter() - t0
+    return 2.0 * job.nx * job.nz * n / el / 1e9, el, threads, kind
+
+
 def run_batched(args, dist):
     """Batched workload: batched persistent engine vs the plain per-shot GPU loop."""
     from das_gb300.batch import BatchEngine
@@ -488,6 +508,15 @@ def run_batched(args, dist):
                           "gpts_per_s": plain_pts / plain_s / 1e9},
            "speedup_vs_plain_loop_gpts": (pts / wall) / (plain_pts / plain_s),
            "autotune": tune_table}
+    if args.cpu_nt > 0:
+        rate, el, threads, kind = cpu_job_rate(jobs[0], args.cpu_nt)
+        cpu_s = pts / (rate * 1e9)
+        out["cpu_baseline"] = {
+            "value": len(jobs) / cpu_s, "unit": "shots/s", "cores": threads, "kind": kind,
+            "sample": f"migrate_shot of gather 0 ({jobs[0].nz}x{jobs[0].nx}) truncated to "
+                      f"nt={min(args.cpu_nt, len(jobs[0].wavelet))}: {rate:.2f} Gpts/s in "
+                      f"{el:.1f} s, extrapolated to the {len(jobs)} gathers' {pts / 1e12:.2f} T "
+                      f"counted points"}
     # roofline of the batch kernel at the device rate: 22 algorithmic bytes per counted
     # point at snapshot interval 2 (16 per step; every second forward step adds 12 for the
     # snapshot and illumination, every second backward step 12 for the imaging)
@@ -670,6 +699,20 @@ def run_served(args, dist):
                 "served_first_jobs": {"p50_latency_s": percentile(served_first, 50),
                                       "p99_latency_s": percentile(served_first, 99)},
                 "speedup_vs_plain_loop_shots": st["shots_per_s"] / plain["shots_per_s"]}
+    if args.cpu_nt > 0:
+        # the reference has a CPU path for the acoustic jobs only (no elastic time loop
+        # or gradient): rate of one acoustic shot, extrapolated to the acoustic shots
+        ac = [r for r in trace if r.kind == "acoustic"]
+        rate, el, threads, kind = cpu_job_rate(ac[0].shots[0], args.cpu_nt)
+        ac_pts = sum(j.counted_points for r in ac for j in r.shots)
+        n_ac = sum(len(r.shots) for r in ac)
+        out_line["cpu_baseline"] = {
+            "value": n_ac / (ac_pts / (rate * 1e9)), "unit": "shots/s", "cores": threads,
+            "kind": kind,
+            "sample": f"acoustic jobs only: migrate_shot of the first acoustic shot truncated to "
+                      f"nt={min(args.cpu_nt, len(ac[0].shots[0].wavelet))}: {rate:.2f} Gpts/s in "
+                      f"{el:.1f} s, extrapolated to the trace's {n_ac} acoustic shots "
+                      f"({ac_pts / 1e12:.2f} T counted points)"}
     print(json.dumps(out_line), flush=True)
 
 
