@@ -394,6 +394,15 @@ __global__ void __launch_bounds__(WARPS * 32)
     grid_dep_launch();
     grid_dep_wait();
     if (threadIdx.x == 0) ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
+    if (s.snap_in && threadIdx.x < T::TZ && z0 + (int)threadIdx.x < g.nz) {
+        // imaging steps read the forward snapshot from HBM after the stencil: start
+        // bringing the tile's rows into L2 now, beside the boxes (one row per thread,
+        // within the row pitch).  (Prefetching the next imaging step's rows one step
+        // ahead as well measured no better.)
+        const int row = z0 + threadIdx.x;
+        prefetch_l2_bulk(s.snap_in + (size_t)row * g.ldx + x0,
+                         (uint32_t)min(AC_TX, g.ldx - x0) * 4u);
+    }
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
     if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {

@@ -134,6 +134,13 @@ __device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* m
         : "memory");
 }
 
+// Bulk prefetch of a contiguous global range into L2 (16-byte aligned address, size a
+// multiple of 16 bytes); no registers or shared memory involved.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Per-thread asynchronous 16-byte copy global -> shared (L2 only), its commit and the
 // wait for all of this thread's copies.  Both addresses 16-byte aligned.
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc)
