@@ -263,6 +263,17 @@ __global__ void __launch_bounds__(WARPS * 32) acoustic_batch_step_kernel(const B
         tma_load_2d(smem + T::C_FLOATS, &mp->prev[pi], x0, z0, bar);
         tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &mp->vel[vi], x0, z0, bar);
     }
+    if ((s.snap_in || s.image || s.illum) && tid < 3 * T::TZ) {
+        // the fused pointwise work reads these planes from HBM after the stencil (a
+        // batch's planes do not stay in L2): bring the tile's rows into L2 beside the
+        // boxes, one row per thread, within the row pitch
+        const int r = tid % T::TZ, f = tid / T::TZ;
+        const float* src = f == 0 ? s.snap_in : (f == 1 ? s.image : s.illum);
+        const int ldx = sh->g.ldx;
+        if (src && z0 + r < sh->g.nz)
+            prefetch_l2_bulk(src + (size_t)(z0 + r) * ldx + x0,
+                             (uint32_t)min(AC_TX, ldx - x0) * 4u);
+    }
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
     if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
