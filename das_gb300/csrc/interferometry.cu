@@ -41,6 +41,7 @@ constexpr int XC_LG = 8;        // lags per thread
 constexpr int XC_WY = 8;        // warps per CTA
 constexpr int XC_LAGS = XC_LG * XC_WY;  // lags per CTA
 constexpr int XC_CHUNK = 1024;  // source samples staged per shared-memory chunk
+static_assert(XC_CHUNK % XC_LG == 0, "chunks hold whole rounds of the register ring");
 
 // Gather the source traces (n_src, nt) and the zero-padded receiver traces
 // (nt + 2*pad, n_rec) out of one (nt, n_ch) data window.
@@ -90,27 +91,37 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
         lo[j] = 0.0f;
         w[j] = Rp[(size_t)(base + j) * n_rec + rr];
     }
+    // The window is a ring of XC_LG registers: sample t's lag j sits in slot
+    // (t + j) % XC_LG, and the slot of R[t] takes R[t + XC_LG] once t is done; the
+    // sample loop is unrolled by XC_LG so every slot index is a constant (no register
+    // moves).  The last chunk is padded with zero source samples to a multiple of
+    // XC_LG: their products are exact zeros and leave the sums unchanged (the rows of
+    // Rp they read lie inside its zero padding).
     for (int t0 = 0; t0 < nt; t0 += XC_CHUNK) {
         const int len = min(XC_CHUNK, nt - t0);
+        const int len_r = (len + XC_LG - 1) / XC_LG * XC_LG;
         __syncthreads();
-        for (int i = threadIdx.y * XC_RX + threadIdx.x; i < len; i += XC_RX * XC_WY)
-            s_src[i] = Ss[t0 + i];
+        for (int i = threadIdx.y * XC_RX + threadIdx.x; i < len_r; i += XC_RX * XC_WY)
+            s_src[i] = i < len ? Ss[t0 + i] : 0.0f;
         __syncthreads();
-        for (int i = 0; i < len; ++i) {
-            const float sv = s_src[i];
+        for (int i0 = 0; i0 < len_r; i0 += XC_LG) {
 #pragma unroll
-            for (int j = 0; j < XC_LG; ++j) {
-                const float p = __fmul_rn(sv, w[j]);
-                const float e = __fmaf_rn(sv, w[j], -p);
-                const float t = __fadd_rn(hi[j], p);
-                const float bp = __fsub_rn(t, hi[j]);
-                const float err = __fadd_rn(__fsub_rn(hi[j], __fsub_rn(t, bp)), __fsub_rn(p, bp));
-                hi[j] = t;
-                lo[j] = __fadd_rn(lo[j], __fadd_rn(err, e));
+            for (int u = 0; u < XC_LG; ++u) {
+                const float sv = s_src[i0 + u];
+#pragma unroll
+                for (int j = 0; j < XC_LG; ++j) {
+                    const float wv = w[(u + j) % XC_LG];
+                    const float p = __fmul_rn(sv, wv);
+                    const float e = __fmaf_rn(sv, wv, -p);
+                    const float t = __fadd_rn(hi[j], p);
+                    const float bp = __fsub_rn(t, hi[j]);
+                    const float err =
+                        __fadd_rn(__fsub_rn(hi[j], __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                    hi[j] = t;
+                    lo[j] = __fadd_rn(lo[j], __fadd_rn(err, e));
+                }
+                w[u] = Rp[(size_t)(base + t0 + i0 + u + XC_LG) * n_rec + rr];
             }
-#pragma unroll
-            for (int j = 0; j < XC_LG - 1; ++j) w[j] = w[j + 1];
-            w[XC_LG - 1] = Rp[(size_t)(base + t0 + i + XC_LG) * n_rec + rr];
         }
     }
     if (r >= n_rec) return;
