@@ -17,11 +17,14 @@
 // added to a float32 stack in window order (the first window is copied), and the
 // stack is divided by float32(number of windows) on request, as the pipeline does.
 //
-// Kernel layout.  One CTA per (source, 64 lags, 32 receivers); a thread owns one
-// receiver and 8 consecutive lags and walks t with an 8-sample sliding window of
-// its receiver trace in registers (the trace is stored zero-padded, so no bounds
-// tests in the loop); the source trace is staged in shared memory in chunks.
-// Receiver-trace loads are coalesced across the 32 receivers of a warp.
+// Kernel layout.  One CTA per (source, 16 lags, 32 receivers); a thread owns one
+// receiver and 8 consecutive lags and walks a quarter of every chunk of t with an
+// 8-sample window of its receiver trace in registers (the trace is stored
+// zero-padded, so no bounds tests in the loop); four warps share a lag group, one per
+// quarter, and their sums are added in quarter order in double-float arithmetic
+// (four times the threads of one warp per lag group: the GPU's FP32 pipes stay fed).
+// The source trace is staged in shared memory in chunks; receiver-trace loads are
+// coalesced across the 32 receivers of a warp.
 #include <math.h>
 #include <string.h>
 
@@ -39,9 +42,12 @@ namespace {
 constexpr int XC_RX = 32;       // receivers per CTA (one per lane)
 constexpr int XC_LG = 8;        // lags per thread
 constexpr int XC_WY = 8;        // warps per CTA
-constexpr int XC_LAGS = XC_LG * XC_WY;  // lags per CTA
+constexpr int XC_TP = 4;        // warps sharing one lag group, each over a quarter of t
+constexpr int XC_LAGS = XC_LG * (XC_WY / XC_TP);  // lags per CTA
 constexpr int XC_CHUNK = 1024;  // source samples staged per shared-memory chunk
-static_assert(XC_CHUNK % XC_LG == 0, "chunks hold whole rounds of the register ring");
+constexpr int XC_PART = XC_CHUNK / XC_TP;  // samples of a chunk per warp
+static_assert(XC_WY % XC_TP == 0 && XC_PART % XC_LG == 0,
+              "every warp's part of a chunk holds whole rounds of the register ring");
 
 // Gather the source traces (n_src, nt) and the zero-padded receiver traces
 // (nt + 2*pad, n_rec) out of one (nt, n_ch) data window.
@@ -70,8 +76,10 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
               int pad, int lag0, int n_rows, float* __restrict__ stack, int first)
 {
     __shared__ float s_src[XC_CHUNK];
+    __shared__ float s_part[XC_WY][2][XC_LG][XC_RX];  // the parts' (hi, lo) sums
     const int r = blockIdx.x * XC_RX + threadIdx.x;
-    const int row0 = blockIdx.y * XC_LAGS + threadIdx.y * XC_LG;
+    const int grp = threadIdx.y % (XC_WY / XC_TP), part = threadIdx.y / (XC_WY / XC_TP);
+    const int row0 = blockIdx.y * XC_LAGS + grp * XC_LG;
     const int s = blockIdx.z;
     const float* Ss = S + (size_t)s * nt;
     const int rr = min(r, n_rec - 1);  // lanes past the last receiver compute a copy
@@ -89,7 +97,6 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
     for (int j = 0; j < XC_LG; ++j) {
         hi[j] = 0.0f;
         lo[j] = 0.0f;
-        w[j] = Rp[(size_t)(base + j) * n_rec + rr];
     }
     // The window is a ring of XC_LG registers: sample t's lag j sits in slot
     // (t + j) % XC_LG, and the slot of R[t] takes R[t + XC_LG] once t is done; the
@@ -104,7 +111,13 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
         for (int i = threadIdx.y * XC_RX + threadIdx.x; i < len_r; i += XC_RX * XC_WY)
             s_src[i] = i < len ? Ss[t0 + i] : 0.0f;
         __syncthreads();
-        for (int i0 = 0; i0 < len_r; i0 += XC_LG) {
+        // this warp's part of the chunk: samples [a, b), its window loaded afresh
+        const int a = part * XC_PART, b = min(len_r, a + XC_PART);
+        if (a < b) {
+#pragma unroll
+            for (int j = 0; j < XC_LG; ++j) w[j] = Rp[(size_t)(base + t0 + a + j) * n_rec + rr];
+        }
+        for (int i0 = a; i0 < b; i0 += XC_LG) {
 #pragma unroll
             for (int u = 0; u < XC_LG; ++u) {
                 const float sv = s_src[i0 + u];
@@ -124,13 +137,30 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
             }
         }
     }
-    if (r >= n_rec) return;
+    // the parts of one lag group add up in part order, in double-float arithmetic
 #pragma unroll
     for (int j = 0; j < XC_LG; ++j) {
+        s_part[threadIdx.y][0][j][threadIdx.x] = hi[j];
+        s_part[threadIdx.y][1][j][threadIdx.x] = lo[j];
+    }
+    __syncthreads();
+    if (part != 0 || r >= n_rec) return;
+#pragma unroll
+    for (int j = 0; j < XC_LG; ++j) {
+        float h = hi[j], l = lo[j];
+        for (int q = 1; q < XC_TP; ++q) {
+            const int wy = q * (XC_WY / XC_TP) + grp;
+            const float ph = s_part[wy][0][j][threadIdx.x], pl = s_part[wy][1][j][threadIdx.x];
+            const float t = __fadd_rn(h, ph);
+            const float bp = __fsub_rn(t, h);
+            const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+            h = t;
+            l = __fadd_rn(l, __fadd_rn(err, pl));
+        }
         const int row = row0 + j;
         if (row >= n_rows) break;
         float* o = stack + ((size_t)s * n_rows + row) * n_rec + r;
-        const float c = __fadd_rn(hi[j], lo[j]);
+        const float c = __fadd_rn(h, l);
         *o = first ? c : __fadd_rn(*o, c);
     }
 }
