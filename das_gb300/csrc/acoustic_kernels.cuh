@@ -509,14 +509,9 @@ inline cudaError_t launch_acoustic_step(const AcMaps& m, const AcGeom& g, const 
                                         cudaStream_t st, int pdl = 0)
 {
     using T = AcTile<WARPS, RPW, SPONGE>;
-    static bool attr_set = false;  // one attribute call per instantiation
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(acoustic_step_kernel<WARPS, RPW, SPONGE>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)T::SMEM_BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e =
+        set_smem_once<acoustic_step_kernel<WARPS, RPW, SPONGE>>((int)T::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
     if (!pdl) {
         acoustic_step_kernel<WARPS, RPW, SPONGE><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);

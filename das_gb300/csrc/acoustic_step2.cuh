@@ -331,14 +331,8 @@ inline cudaError_t launch_acoustic_step2_t(const Ac2Maps& m, const AcGeom& g, co
                                            cudaStream_t st, int pdl)
 {
     using T = Ac2Tile<R2, SPONGE>;
-    static bool attr_set = false;  // one attribute call per instantiation
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(acoustic_step2_kernel<R2, SPONGE>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)T::SMEM_BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = set_smem_once<acoustic_step2_kernel<R2, SPONGE>>((int)T::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
     return launch_ex(acoustic_step2_kernel<R2, SPONGE>, grid, dim3(128), T::SMEM_BYTES, st, pdl, m,
                      g, p);

@@ -140,14 +140,8 @@ inline cudaError_t launch_adjoint_step(const AdjMaps& m, const AcGeom& g, const 
                                        cudaStream_t st)
 {
     using T = AdjTile<WARPS, RPW>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(acoustic_adjoint_kernel<WARPS, RPW>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)T::SMEM_BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = set_smem_once<acoustic_adjoint_kernel<WARPS, RPW>>((int)T::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
     acoustic_adjoint_kernel<WARPS, RPW><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
     return cudaGetLastError();

@@ -151,15 +151,7 @@ template <int W, int R>
 cudaError_t batch_step_attr()
 {
     using T = AcTile<W, R, SPONGE_LUT>;
-    static bool attr_set = false;  // one attribute call per instantiation
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(acoustic_batch_step_kernel<W, R>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)T::SMEM_BYTES);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    return cudaSuccess;
+    return set_smem_once<acoustic_batch_step_kernel<W, R>>((int)T::SMEM_BYTES);
 }
 
 cudaError_t batch_step_attr_cfg(const w2d_batch* b)

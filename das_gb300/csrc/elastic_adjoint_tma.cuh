@@ -428,13 +428,8 @@ cudaError_t launch_el_adj_a_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
 {
     using T = ElAdjTile<WARPS, RPW>;
     const int bytes = T::A_FLOATS * 4 + 128;
-    static bool attr_set = false;  // one attribute call per process and shape
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(el_adj_a<WARPS, RPW>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = set_smem_once<el_adj_a<WARPS, RPW>>(bytes);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
     return el_launch(el_adj_a<WARPS, RPW>, grid, dim3(WARPS * 32), bytes, st, pdl, m, g, p, sd, a,
                      r, glam, gmu, gbx, gbz, rv, err);
@@ -447,13 +442,8 @@ cudaError_t launch_el_adj_b_t(const ElAdjMaps& m, const ElGeom& g, const ElParam
 {
     using T = ElAdjTile<WARPS, RPW>;
     const int bytes = T::B_FLOATS * 4 + 128;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(el_adj_b<WARPS, RPW>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = set_smem_once<el_adj_b<WARPS, RPW>>(bytes);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
     return el_launch(el_adj_b<WARPS, RPW>, grid, dim3(WARPS * 32), bytes, st, pdl, m, g, p, sd, a,
                      t, then_k1, err);

@@ -506,19 +506,12 @@ cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElS
 {
     using T = ElTile<WARPS, RPW>;
     const int vbytes = T::V_FLOATS * 4 + 128, sbytes = T::S_FLOATS * 4 + 128;
-    static bool attr_set = false;  // one attribute call per process and shape
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(elastic_velocity_kernel<WARPS, RPW>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, vbytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(elastic_stress_kernel<WARPS, RPW>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, sbytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    cudaError_t e = set_smem_once<elastic_velocity_kernel<WARPS, RPW>>(vbytes);
+    if (e == cudaSuccess) e = set_smem_once<elastic_stress_kernel<WARPS, RPW>>(sbytes);
+    if (e != cudaSuccess) return e;
     dim3 grid((g.nx + EL_TX - 1) / EL_TX, (g.nz + T::TZ - 1) / T::TZ, n_shots);
-    cudaError_t e = el_launch(elastic_velocity_kernel<WARPS, RPW>, grid, dim3(WARPS * 32),
-                              vbytes, st, pdl, maps, g, s);
+    e = el_launch(elastic_velocity_kernel<WARPS, RPW>, grid, dim3(WARPS * 32), vbytes, st, pdl,
+                  maps, g, s);
     if (e != cudaSuccess) return e;
     ElStep s2 = s;
     s2.src_pos = nullptr;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 
 #include "wave2d_cuda.h"
@@ -215,6 +216,19 @@ __device__ __forceinline__ void grid_dep_launch()
 __device__ __forceinline__ void grid_dep_wait()
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Raise a kernel's dynamic shared-memory limit once per process: one flag per kernel
+// (the kernel is the template argument), safe when several host threads launch it.
+template <auto Kernel>
+inline cudaError_t set_smem_once(int bytes)
+{
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [bytes] {
+        err = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    });
+    return err;
 }
 
 // IEEE single-precision arithmetic with no contraction into FMA: the engine
