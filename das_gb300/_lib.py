@@ -91,6 +91,7 @@ _SIGS = {
     "w2d_elastic_set_adjoint": (c_int, [c_void_p, c_int]),
     "w2d_elastic_set_tiles": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),
     "w2d_elastic_set_pdl": (c_int, [c_void_p, c_int]),
+    "w2d_elastic_share_model": (c_int, [c_void_p, c_int]),
     "w2d_batch_create": (c_int, [ctypes.POINTER(c_void_p), c_ull, c_int]),
     "w2d_batch_destroy": (None, [c_void_p]),
     "w2d_batch_set_config": (c_int, [c_void_p, c_int, c_int, c_int, c_int]),

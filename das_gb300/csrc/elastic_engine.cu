@@ -60,6 +60,11 @@ struct w2d_elastic {
     CUtensorMap map_state;                  // 3D map over the S x 5 planes of `state`
     std::vector<CUtensorMap> seg_maps;      // one per slot of `seg`
     int adj_form = 1;                       // 1: TMA-tiled adjoint passes, 0: per-cell kernels
+    // every shot of the next batch has the same model: its parameters are stored once and
+    // read by every shot (parameter stride 0), so a tile's parameters come from L2 for
+    // all but the first shot to touch them
+    int shared_next = 0;
+    size_t pstride = 0;                     // parameter stride per shot of the current batch
     int fwd_warps = EL_WARPS, fwd_rpw = EL_RPW;          // step kernels' tile
     int adj_warps = EL_ADJ_WARPS, adj_rpw = EL_ADJ_RPW;  // adjoint passes' tile
     // the tiles the current maps were made for (a change applies at the next forward)
@@ -122,7 +127,7 @@ ElParams eparams(w2d_elastic* e)
 
 ElStrides estrides(w2d_elastic* e)
 {
-    return ElStrides{e->SS(), 4 * e->plane, 4 * e->plane};
+    return ElStrides{e->SS(), e->pstride, 4 * e->plane};
 }
 
 // Step n of every shot from the states at src to the states at dst (same pointer:
@@ -141,7 +146,7 @@ int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, c
     st.mu = e->P(0, 1);
     st.bx = e->P(0, 2);
     st.bz = e->P(0, 3);
-    st.pstride = 4 * e->plane;
+    st.pstride = e->pstride;
     st.src_pos = e->src_pos;
     st.wav = e->wav;
     st.nt = e->nt;
@@ -315,7 +320,10 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
             return rc;
     const size_t hp = (size_t)e->nx * 4, dp = (size_t)e->ldx * 4, np = (size_t)e->nx * e->nz;
     const float* src[4] = {lam, mu, bx, bz};
-    for (int s = 0; s < S; ++s)
+    const int n_models = e->shared_next ? 1 : S;
+    e->pstride = e->shared_next ? 0 : 4 * P;
+    e->shared_next = 0;  // one batch only
+    for (int s = 0; s < n_models; ++s)
         for (int i = 0; i < 4; ++i)
             W2D_CUDA_TRY(cudaMemcpy2DAsync(e->P(s, i), dp, src[i] + (size_t)s * np, hp, hp, e->nz,
                                            cudaMemcpyDeviceToDevice, e->st));
@@ -480,6 +488,13 @@ int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
 {
     W2D_CHECK_ARG(e && (form == 0 || form == 1), "form must be 0 (per-cell) or 1 (tiled)");
     e->adj_form = form;
+    return W2D_OK;
+}
+
+int w2d_elastic_share_model(w2d_elastic* e, int on)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    e->shared_next = on ? 1 : 0;
     return W2D_OK;
 }
 

@@ -33,6 +33,8 @@ class ElasticSolver2D:
                                                 n_sponge, self.sponge_alpha,
                                                 1 if free_surface_top else 0))
         self._h = h
+        # a batch whose shots have identical models stores and reads one copy
+        self.share_models = True
 
     def close(self):
         if getattr(self, "_h", None) is not None:
@@ -110,6 +112,10 @@ class ElasticModeling(torch.autograd.Function):
         rix = normalize_indices(receiver_ix, solver.nx, "receiver_ix")
         riz = normalize_index(receiver_iz, solver.nz, "receiver_iz")
         traces = torch.empty((S, nt, len(rix)), dtype=torch.float32, device=ps[0].device)
+        # shots of one model (a job's shots, as in a survey): store and read it once
+        shared = batched and S > 1 and solver.share_models and all(
+            bool(torch.equal(t, t[:1].expand_as(t))) for t in ps)
+        _lib.check(solver._lib.w2d_elastic_share_model(solver._h, 1 if shared else 0))
         torch.cuda.current_stream(ps[0].device).synchronize()
         _lib.check(solver._lib.w2d_elastic_forward_batch(
             solver._h, S, *[t.data_ptr() for t in ps], w.ctypes.data, nt, six.ctypes.data,

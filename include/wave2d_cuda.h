@@ -230,6 +230,11 @@ int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp
  * (on by default; each kernel's set-up overlaps its predecessor's tail, and it waits
  * for the predecessor before any global access).  Results are identical either way. */
 int w2d_elastic_set_pdl(w2d_elastic* e, int on);
+/* The next w2d_elastic_forward_batch's shots all have the same model (the caller has
+ * checked): only the first shot's lam, mu, bx, bz are read and stored, and every shot
+ * reads them (their tiles then come from L2 for all but the first shot).  Gradients
+ * stay per shot.  Applies to that one call. */
+int w2d_elastic_share_model(w2d_elastic* e, int on);
 /* Device bytes one shot of a batch holds (checkpoints, one recomputed segment, fields). */
 unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 

@@ -193,3 +193,25 @@ def test_programmatic_dependent_launch_does_not_change_results():
     solver.set_pdl(True)
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
+def test_shared_model_batch_equals_separate_copies():
+    """Shots of one model: the batch stores the model once and every shot reads it
+    (parameter stride 0); traces and per-shot gradients bit-identical to the batch with
+    one copy per shot."""
+    from das_gb300.elastic import elastic_traces
+    torch, solver, grid, w, rix = _setup()
+    vs, _ = _model()
+    R = torch.tensor(np.random.default_rng(6).standard_normal((3, len(w), len(rix))).astype(
+        np.float32), device="cuda")
+    out = []
+    for share in (True, False):
+        solver.share_models = share
+        v = torch.tensor(np.stack([vs, vs, vs]), device="cuda", requires_grad=True)
+        d = elastic_traces(v, solver, np.stack([w, w * 0.5, w]), [15, 40, 60], [3, 3, 4], rix, 2)
+        (d * R).sum().backward()
+        out.append((d.detach().cpu().numpy(), v.grad.cpu().numpy()))
+    solver.share_models = True
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert not np.array_equal(out[0][1][0], out[0][1][1])  # per-shot gradients differ
