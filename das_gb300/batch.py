@@ -30,7 +30,7 @@ class _ShotDesc(ctypes.Structure):
                 ("src_ix", ctypes.c_int), ("src_iz", ctypes.c_int), ("rec_iz", ctypes.c_int),
                 ("vel_fwd", ctypes.c_void_p), ("vel_bwd", ctypes.c_void_p),
                 ("wavelet", ctypes.c_void_p), ("data", ctypes.c_void_p),
-                ("rec_ix", ctypes.c_void_p)]
+                ("rec_ix", ctypes.c_void_p), ("model_key", ctypes.c_longlong)]
 
 
 @dataclass
@@ -54,6 +54,9 @@ class ShotJob:
     sponge_alpha: float = 0.0015
     free_surface_top: bool = True
     tag: object = None
+    # nonzero: every job submitted with this key has identical models (the shots of one
+    # survey); the engine keeps one device copy of them while any such job is admitted
+    model_key: int = 0
     _keep: list = field(default_factory=list, repr=False)
 
     def desc(self) -> _ShotDesc:
@@ -76,7 +79,8 @@ class ShotJob:
                          normalize_index(self.source_iz, self.nz, "source_iz"),
                          normalize_index(self.receiver_iz, self.nz, "receiver_iz"),
                          vf.ctypes.data, vb.ctypes.data, w.ctypes.data,
-                         data.ctypes.data if data.size else None, rix.ctypes.data)
+                         data.ctypes.data if data.size else None, rix.ctypes.data,
+                         int(self.model_key))
 
     @property
     def counted_points(self) -> int:
@@ -102,6 +106,9 @@ class ModelJob:
     sponge_alpha: float = 0.0015
     free_surface_top: bool = True
     tag: object = None
+    # nonzero: every job submitted with this key has identical models (the shots of one
+    # survey); the engine keeps one device copy of them while any such job is admitted
+    model_key: int = 0
     _keep: list = field(default_factory=list, repr=False)
 
     def desc(self) -> _ShotDesc:
@@ -118,7 +125,7 @@ class ModelJob:
                          normalize_index(self.source_iz, self.nz, "source_iz"),
                          normalize_index(self.receiver_iz, self.nz, "receiver_iz"),
                          v.ctypes.data, None, w.ctypes.data, None,
-                         rix.ctypes.data if len(rix) else None)
+                         rix.ctypes.data if len(rix) else None, int(self.model_key))
 
     @property
     def n_receivers(self) -> int:

@@ -34,6 +34,7 @@ constexpr size_t kAlign = 256;
 struct HostShot {
     bool used = false, finished = false;
     size_t off = 0, bytes = 0;  // arena block
+    long long model_key = 0;    // nonzero: the models live in a shared model block
     int nx = 0, nz = 0, ldx = 0;
     size_t plane = 0;
     int k0 = 0, k_end = 0;
@@ -44,6 +45,14 @@ struct HostShot {
     int mode = 0;            // 0: migration, 1: forward modelling
     int nt = 0, n_rec = 0;
     float* traces = nullptr;  // mode 1: (nt, n_rec)
+};
+
+// Device copy of models shared by the shots submitted with one model key.
+struct ModelBlock {
+    size_t off = 0, bytes = 0;
+    int refs = 0;
+    int nx = 0, nz = 0, n_models = 0;
+    double dt = 0;
 };
 
 }  // namespace
@@ -66,6 +75,7 @@ struct w2d_batch {
     unsigned* d_err = nullptr;
     std::vector<BShot> h_shots;
     std::vector<HostShot> hs;
+    std::map<long long, ModelBlock> models;  // by model key
     std::vector<int> active;
     bool active_dirty = true;
     int warps = 8, rpw = 4, S = 16, chunks = 8;
@@ -481,20 +491,39 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
         cur += (bytes + kAlign - 1) / kAlign * kAlign;
         return o;
     };
-    const size_t o_wave = take(n_waves * plane * 4), o_vel = take(n_models * plane * 4),
+    const long long key = d->model_key;
+    ModelBlock* shared = nullptr;
+    if (key) {
+        auto it = b->models.find(key);
+        if (it != b->models.end()) {
+            const ModelBlock& m = it->second;
+            W2D_CHECK_ARG(m.nx == nx && m.nz == nz && m.n_models == n_models && m.dt == d->dt,
+                          "a model key given to jobs of different grids, steps or kinds");
+            shared = &it->second;
+        }
+    }
+    const size_t o_wave = take(n_waves * plane * 4), o_vel = take(key ? 0 : n_models * plane * 4),
                  o_img = take(n_img * plane * 4), o_ill = take(n_img * plane * 4),
                  o_snap = take(n_snaps * plane * 4), o_w = take((size_t)nt * 4),
                  o_data = take((size_t)nt * std::max(n_rec, 1) * 4), o_lut = take((n_sp + 1) * 4),
                  o_ptr = take((nx + 1) * 4), o_list = take(std::max(n_rec, 1) * 4),
                  o_done = take((size_t)tiles_x * tiles_z * 4);
-    size_t off = 0;
+    size_t off = 0, moff = 0;
+    const size_t mbytes = (size_t)n_models * plane * 4;
     if (!arena_alloc(b, cur, &off)) {
         set_error("not enough arena memory for this shot now");
         return W2D_ENOMEM;
     }
+    if (key && !shared && !arena_alloc(b, mbytes, &moff)) {  // the key's first shot
+        arena_free(b, off, cur);
+        set_error("not enough arena memory for this shot now");
+        return W2D_ENOMEM;
+    }
+    const bool own_model_block = key && !shared;
     char* base = b->arena + off;
     float* wave = reinterpret_cast<float*>(base + o_wave);
-    float* vel = reinterpret_cast<float*>(base + o_vel);
+    float* vel = key ? reinterpret_cast<float*>(b->arena + (shared ? shared->off : moff))
+                     : reinterpret_cast<float*>(base + o_vel);
     float* img = reinterpret_cast<float*>(base + o_img);
     float* ill = reinterpret_cast<float*>(base + o_ill);
     float* snaps = reinterpret_cast<float*>(base + o_snap);
@@ -510,6 +539,7 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
     int rc = W2D_OK;
     auto undo = [&](int code) {
         arena_free(b, off, cur);
+        if (own_model_block) arena_free(b, moff, mbytes);
         return code;
     };
     // host-side tables
@@ -532,7 +562,7 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
         cudaMemsetAsync(base + o_img, 0, o_snap - o_img, st) != cudaSuccess ||
         cudaMemsetAsync(base + o_done, 0, cur - o_done, st) != cudaSuccess)
         return undo(W2D_ECUDA);
-    for (int m = 0; m < n_models; ++m) {
+    for (int m = 0; m < (shared ? 0 : n_models); ++m) {  // a shared copy is there already
         const float* hv = m == 0 ? d->vel_fwd : d->vel_bwd;
         if (cudaMemcpy2DAsync(stage, (size_t)ldx * 4, hv, (size_t)nx * 4, (size_t)nx * 4, nz,
                               cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -614,11 +644,27 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
         set_error("shot admission failed on the device");
         return undo(W2D_ECUDA);
     }
+    if (key) {
+        if (shared) {
+            shared->refs++;
+        } else {
+            ModelBlock m;
+            m.off = moff;
+            m.bytes = mbytes;
+            m.refs = 1;
+            m.nx = nx;
+            m.nz = nz;
+            m.n_models = n_models;
+            m.dt = d->dt;
+            b->models[key] = m;
+        }
+    }
     HostShot& hsh = b->hs[slot];
     hsh = HostShot();
     hsh.used = true;
     hsh.off = off;
     hsh.bytes = cur;
+    hsh.model_key = key;
     hsh.nx = nx;
     hsh.nz = nz;
     hsh.ldx = ldx;
@@ -790,6 +836,22 @@ int w2d_batch_is_finished(w2d_batch* b, int slot)
     return b->hs[slot].finished ? 1 : 0;
 }
 
+// Give a retired shot's memory back: its block, and its shared models once no admitted
+// shot uses them.
+static void release_shot(w2d_batch* b, int slot)
+{
+    HostShot& h = b->hs[slot];
+    arena_free(b, h.off, h.bytes);
+    if (h.model_key) {
+        auto it = b->models.find(h.model_key);
+        if (it != b->models.end() && --it->second.refs == 0) {
+            arena_free(b, it->second.off, it->second.bytes);
+            b->models.erase(it);
+        }
+    }
+    h = HostShot();
+}
+
 int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
 {
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
@@ -806,8 +868,7 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
         W2D_CUDA_TRY(cudaMemcpy2DAsync(illum_out, hp, h.illum, dp, hp, h.nz,
                                        cudaMemcpyDeviceToHost, b->st_up));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
-    arena_free(b, h.off, h.bytes);
-    h = HostShot();
+    release_shot(b, slot);
     return W2D_OK;
 }
 
@@ -821,8 +882,7 @@ int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out)
         W2D_CUDA_TRY(cudaMemcpyAsync(traces_out, h.traces, (size_t)h.nt * h.n_rec * 4,
                                      cudaMemcpyDeviceToHost, b->st_up));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
-    arena_free(b, h.off, h.bytes);
-    h = HostShot();
+    release_shot(b, slot);
     return W2D_OK;
 }
 
@@ -839,8 +899,7 @@ int w2d_batch_cancel(w2d_batch* b, int slot)
     if (jt != b->joining.end()) b->joining.erase(jt);
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st_up));
     W2D_CUDA_TRY(cudaStreamSynchronize(b->st));
-    arena_free(b, b->hs[slot].off, b->hs[slot].bytes);
-    b->hs[slot] = HostShot();
+    release_shot(b, slot);
     return W2D_OK;
 }
 

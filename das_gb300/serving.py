@@ -17,6 +17,7 @@ and returning its per-shot results) between replays when one is given.
 from __future__ import annotations
 
 import collections
+import itertools
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional, Sequence
@@ -49,6 +50,24 @@ class RTMResponse:
 
 def percentile(xs: Sequence[float], q: float) -> float:
     return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else float("nan")
+
+
+_MODEL_KEYS = itertools.count(1)
+
+
+def share_models(shots) -> None:
+    """Give the shots of one request that hold the same model arrays (the same objects)
+    one model key, so the batch engine keeps a single device copy of those models while
+    any of the shots is admitted.  Shots that already carry a key keep it."""
+    groups = {}
+    for sh in shots:
+        if getattr(sh, "model_key", 0):
+            continue
+        ident = (id(getattr(sh, "vel_fwd", None)), id(getattr(sh, "vel_bwd", None)),
+                 id(getattr(sh, "vel", None)))
+        if ident not in groups:
+            groups[ident] = next(_MODEL_KEYS)
+        sh.model_key = groups[ident]
 
 
 class RTMServer:
@@ -91,6 +110,7 @@ class RTMServer:
                 if req.kind == "elastic" and self.elastic_executor is not None:
                     self.elastic_executor.submit(req)
                 else:
+                    share_models(req.shots)
                     for k in range(len(req.shots)):
                         queue.append((req, k))
                 i += 1

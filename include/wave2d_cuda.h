@@ -243,7 +243,11 @@ unsigned long long w2d_elastic_shot_bytes(int nx, int nz, int nt, int n_rec);
 
 /* One shot's migration job: grid, Cerjan sponge parameters (n_sponge < 0: no
  * sponge), models (vel_fwd = sediment flood, vel_bwd = rock flood), wavelet (nt),
- * data (nt, n_rec), receiver columns; host arrays, copied at submission. */
+ * data (nt, n_rec), receiver columns; host arrays, copied at submission.
+ * model_key: 0, or a key the caller gives every shot whose models are identical (the
+ * shots of one job): while any shot with the key is admitted, later shots with the
+ * same key (same grid, dt and job kind) use its device copy of the models instead of
+ * their own, so one job's shots read one model. */
 typedef struct {
     int nx, nz;
     float dx, dz;
@@ -258,6 +262,7 @@ typedef struct {
     const float* wavelet;
     const float* data;
     const int* rec_ix;
+    long long model_key;
 } w2d_shot_desc;
 
 typedef struct w2d_batch w2d_batch;

@@ -145,3 +145,49 @@ def test_batch_modelling_matches_engine_forward():
         ref, _ = s.forward_propagate_acoustic(j.vel, j.wavelet, j.source_ix, j.source_iz,
                                               j.receiver_ix, j.receiver_iz, False)
         np.testing.assert_array_equal(tr, ref)
+
+
+@pytest.mark.parametrize("form", ["grid", "queue"])
+def test_shots_sharing_a_model_key(form):
+    """Six shots of one survey (one model pair, one key) plus a modelling job and an
+    unkeyed shot, in an arena that admits only part of them at a time: every result
+    equals the shot migrated alone, the shared model block is released with its last
+    shot (the arena is whole again), and a key reused for another grid is refused."""
+    import dataclasses
+    from das_gb300._lib import W2DError
+    from das_gb300.batch import BatchEngine, ModelJob
+    base = _job(11, 80, 300, 140)
+    rng = np.random.default_rng(12)
+    jobs = []
+    for k in range(6):
+        data = (rng.standard_normal(base.data.shape) * 1e-7).astype(np.float32)
+        jobs.append(dataclasses.replace(base, data=data, source_ix=int(20 + 40 * k),
+                                        model_key=77))
+    jobs.append(ModelJob(base.nx, base.nz, base.dx, base.dz, base.dt, base.vel_fwd, base.wavelet,
+                         base.receiver_ix, 150, 3, 2, base.n_sponge, base.sponge_alpha, True,
+                         model_key=78))
+    jobs.append(_job(13, 50, 200, 90))
+    per = max(BatchEngine.shot_bytes(j) for j in jobs)
+    eng = BatchEngine(arena_bytes=int(3.2 * per), max_shots=8, tile=(4, 4), form=form)
+    whole = eng.free_bytes()
+    results, _ = eng.run(jobs)
+    for j, res in zip(jobs, results):
+        if isinstance(j, ModelJob):
+            from das_gb300.wave_solver import WaveSolver2D
+            s = WaveSolver2D(j.nx, j.nz, j.dx, j.dz, j.dt, j.n_sponge, j.sponge_alpha, True)
+            want, _ = s.forward_propagate_acoustic(j.vel, j.wavelet, j.source_ix, j.source_iz,
+                                                   j.receiver_ix, j.receiver_iz)
+            np.testing.assert_array_equal(res, want)
+            s.close()
+        else:
+            ref_img, ref_ill = _alone(j)
+            np.testing.assert_array_equal(res[0], ref_img)
+            np.testing.assert_array_equal(res[1], ref_ill)
+    assert eng.free_bytes() == whole
+    bad = dataclasses.replace(_job(14, 60, 120, 50), model_key=77)
+    slot = eng.submit(dataclasses.replace(jobs[0]))
+    with pytest.raises(W2DError):
+        eng.submit(bad)
+    eng.wait()
+    eng.close()
+    assert slot is not None
