@@ -13,6 +13,7 @@ cell is the same fused step, independent of what else is in the batch.
 from __future__ import annotations
 
 import ctypes
+import itertools
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Tuple
 
@@ -20,6 +21,14 @@ import numpy as np
 
 from . import _lib
 from .geometry import normalize_index, normalize_indices
+
+
+_KEYS = itertools.count(1)
+
+
+def new_model_key() -> int:
+    """A model key no other job of this process has been given."""
+    return next(_KEYS)
 
 
 class _ShotDesc(ctypes.Structure):

@@ -150,9 +150,10 @@ class TSWRTMEngine:
                          source_coords_iz, receiver_gathers, receiver_ix, receiver_iz,
                          snapshot_interval) -> bool:
         """All shots as one batch; False (nothing done) when one shot does not fit."""
-        from .batch import BatchEngine, ShotJob
+        from .batch import BatchEngine, ShotJob, new_model_key
         s = self.solver
         n_sp = s.n_sponge if s.sponge is not None else -1
+        key = new_model_key()  # every shot migrates in the same flood models
         jobs = []
         for k in range(len(source_coords_ix)):
             w, data, rix, riz, six, siz = self._check(receiver_gathers[k], receiver_ix,
@@ -161,7 +162,7 @@ class TSWRTMEngine:
             jobs.append(ShotJob(s.nx, s.nz, s.dx, s.dz, s.dt, flood_models.sediment_flood,
                                 flood_models.rock_flood, w, data, rix, six, siz, riz,
                                 int(snapshot_interval), n_sp, s.sponge_alpha,
-                                bool(s.free_surface_top)))
+                                bool(s.free_surface_top), model_key=key))
         per = max(BatchEngine.shot_bytes(j) for j in jobs)
         free, _ = _lib.device_memory()
         arena = min(per * len(jobs), int(0.5 * free) + self._batch_arena)

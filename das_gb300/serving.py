@@ -17,14 +17,13 @@ and returning its per-shot results) between replays when one is given.
 from __future__ import annotations
 
 import collections
-import itertools
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional, Sequence
 
 import numpy as np
 
-from .batch import BatchEngine, ShotJob
+from .batch import BatchEngine, ShotJob, new_model_key
 
 
 @dataclass
@@ -52,9 +51,6 @@ def percentile(xs: Sequence[float], q: float) -> float:
     return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else float("nan")
 
 
-_MODEL_KEYS = itertools.count(1)
-
-
 def share_models(shots) -> None:
     """Give the shots of one request that hold the same model arrays (the same objects)
     one model key, so the batch engine keeps a single device copy of those models while
@@ -66,7 +62,7 @@ def share_models(shots) -> None:
         ident = (id(getattr(sh, "vel_fwd", None)), id(getattr(sh, "vel_bwd", None)),
                  id(getattr(sh, "vel", None)))
         if ident not in groups:
-            groups[ident] = next(_MODEL_KEYS)
+            groups[ident] = new_model_key()
         sh.model_key = groups[ident]
 
 
