@@ -307,3 +307,32 @@ def test_errors_are_raised():
     rec_pos, _ = s.forward_propagate_acoustic(vel, w + 1, 63, 2, np.array([63, 0]), 2)
     np.testing.assert_array_equal(rec_neg, rec_pos)
     assert issubclass(W2DError, RuntimeError)
+
+
+@pytest.mark.parametrize("nz,nx,nt,n_rec", [(5, 5, 1, 0), (5, 9, 7, 0), (6, 37, 13, 1), (41, 5, 9, 3)])
+def test_degenerate_sizes_vs_oracle(nz, nx, nt, n_rec):
+    """The smallest grids the engine takes, one-step runs and runs without receivers:
+    traces, snapshots, image and illumination equal the oracle's (an empty receiver set
+    gives (nt, 0) traces and a zero image)."""
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.velocity_flood import FloodModels
+    rng = np.random.default_rng(nz * 100 + nx)
+    grid = o.Grid(nx, nz, 10.0, 10.0, 1e-3, 2, 0.01, True)
+    vel = rng.uniform(1500, 2500, (nz, nx)).astype(np.float32)
+    w = rng.standard_normal(nt).astype(np.float32)
+    rix = np.sort(rng.integers(0, nx, size=n_rec))
+    s = _solver(grid)
+    rec, snaps = s.forward_propagate_acoustic(vel, w, nx // 2, 2, rix, 2, True, 1)
+    rec_o, snaps_o = o.forward_propagate_acoustic(grid, vel, w, nx // 2, 2, rix, 2, True, 1)
+    assert rec.shape == (nt, n_rec)
+    np.testing.assert_array_equal(rec, rec_o)
+    np.testing.assert_array_equal(snaps, snaps_o)
+    data = (rng.standard_normal((nt, n_rec)) * 1e-3).astype(np.float32)
+    fm = FloodModels(vel, vel, vel, 0, 0)
+    img, ill = TSWRTMEngine(s).migrate_shot(fm, w, nx // 2, 2, data, rix, 2, 1)
+    img_o, ill_o = o.migrate_shot(grid, vel, vel, w, nx // 2, 2, data, rix, 2, 1)
+    np.testing.assert_array_equal(img, img_o)
+    np.testing.assert_array_equal(ill, ill_o)
+    if n_rec == 0:
+        assert not img.any()
+    s.close()
