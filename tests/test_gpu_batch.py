@@ -191,3 +191,22 @@ def test_shots_sharing_a_model_key(form):
     eng.wait()
     eng.close()
     assert slot is not None
+
+
+def test_batch_shot_without_receivers_and_one_step():
+    """A shot with no receivers (zero image) and a one-step shot beside an ordinary one:
+    each equals the shot migrated alone."""
+    import dataclasses
+    from das_gb300.batch import BatchEngine
+    a = _job(21, 40, 100, 60)
+    b = dataclasses.replace(_job(22, 30, 90, 40), data=np.zeros((40, 0), np.float32),
+                            receiver_ix=np.zeros(0, dtype=np.int64))
+    c = _job(23, 25, 70, 1)
+    eng = BatchEngine(arena_bytes=1 << 28, max_shots=4, tile=(4, 4))
+    results, _ = eng.run([a, b, c])
+    for j, (img, ill) in zip([a, b, c], results):
+        ref_img, ref_ill = _alone(j)
+        np.testing.assert_array_equal(img, ref_img)
+        np.testing.assert_array_equal(ill, ref_ill)
+    assert not results[1][0].any()
+    eng.close()
