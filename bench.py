@@ -22,6 +22,18 @@ per shot (forward + backward; recomputation not counted).
   restated in oracle/) timed on this host's cores over a bounded sample.
 * ``--impl reference``: that CPU implementation alone, each step a bounded sample
   of the same workload (rank 0 only).
+
+Other workloads (``--workload``), one JSON line each:
+
+* ``small``: the reference's own example size (150 x 400, nt 2000, 20 shots), the whole
+  ``TSWRTMEngine.migrate_multiple_shots`` call against the per-shot loop and the CPU path
+  over all 20 shots.
+* ``batched``: 256 uneven virtual-source gathers through the batch engine against the
+  plain per-shot loop (shots/s).
+* ``served``: a Poisson trace of acoustic and elastic jobs through the server against the
+  plain FIFO per-shot loop (shots/s, p50 / p99 latency).
+* ``elastic``: one elastic shot's forward modelling and exact adjoint gradient.
+* ``interferometry``: virtual-source cross-correlation stacking (windows/s).
 """
 from __future__ import annotations
 
