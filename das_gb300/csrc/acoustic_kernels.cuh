@@ -528,26 +528,30 @@ constexpr size_t persistent_smem_bytes()
     return 2 * AcTile<WARPS, RPW, SPONGE>::FLOATS * 4u + 128;
 }
 
-// Resident CTAs of the persistent form on the current device (0 on error).
+// Resident CTAs of the persistent form on the current device (0 on error): one query
+// per instantiation and device, safe when several host threads ask.
 template <int WARPS, int RPW, int SPONGE>
 inline int persistent_capacity()
 {
-    static int cap = -1;  // one query per instantiation
-    if (cap < 0) {
+    auto query = [](int dev) {
         const int smem = (int)persistent_smem_bytes<WARPS, RPW, SPONGE>();
-        if (cudaFuncSetAttribute(acoustic_step_persistent<WARPS, RPW, SPONGE>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        if (set_smem_once<acoustic_step_persistent<WARPS, RPW, SPONGE>>(smem) != cudaSuccess)
             return 0;
-        int per_sm = 0, dev = 0, sms = 0;
+        int per_sm = 0, sms = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                 &per_sm, acoustic_step_persistent<WARPS, RPW, SPONGE>, WARPS * 32, smem) !=
-            cudaSuccess)
+                cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cap = per_sm * sms;
-    }
-    return cap;
+        return per_sm * sms;
+    };
+    static std::once_flag once[W2D_MAX_DEVICES];
+    static int cap[W2D_MAX_DEVICES];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (dev < 0 || dev >= W2D_MAX_DEVICES) return query(dev);
+    std::call_once(once[dev], [&query, dev] { cap[dev] = query(dev); });
+    return cap[dev];
 }
 
 // One persistent launch; *base is advanced by the indices the launch draws.

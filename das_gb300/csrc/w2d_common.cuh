@@ -218,17 +218,29 @@ __device__ __forceinline__ void grid_dep_wait()
     asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
-// Raise a kernel's dynamic shared-memory limit once per process: one flag per kernel
-// (the kernel is the template argument), safe when several host threads launch it.
+// Device ordinals covered by the per-device caches below; a device beyond them has
+// its attributes set on every call instead.
+constexpr int W2D_MAX_DEVICES = 64;
+
+// Raise a kernel's dynamic shared-memory limit once per device (the attribute belongs
+// to the kernel as loaded on one device, and one process may drive several devices
+// through w2d_set_device): one flag per kernel (the template argument) and device,
+// safe when several host threads launch it.  bytes is fixed per kernel.
 template <auto Kernel>
 inline cudaError_t set_smem_once(int bytes)
 {
-    static std::once_flag once;
-    static cudaError_t err = cudaSuccess;
-    std::call_once(once, [bytes] {
-        err = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    static std::once_flag once[W2D_MAX_DEVICES];
+    static cudaError_t err[W2D_MAX_DEVICES];  // zero-initialised: cudaSuccess
+    int dev = 0;
+    const cudaError_t ge = cudaGetDevice(&dev);
+    if (ge != cudaSuccess) return ge;
+    if (dev < 0 || dev >= W2D_MAX_DEVICES)
+        return cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    std::call_once(once[dev], [bytes, dev] {
+        err[dev] = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        bytes);
     });
-    return err;
+    return err[dev];
 }
 
 // IEEE single-precision arithmetic with no contraction into FMA: the engine
