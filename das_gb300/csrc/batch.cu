@@ -58,6 +58,7 @@ struct ModelBlock {
 }  // namespace
 
 struct w2d_batch {
+    int device = 0;  // CUDA device current at creation: every call on the handle runs there
     cudaStream_t st = nullptr;     // replays of the captured time loop
     cudaStream_t st_up = nullptr;  // shot admission (uploads, set-up kernels)
     char* arena = nullptr;
@@ -313,6 +314,7 @@ int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_sh
     W2D_CHECK_ARG(out && max_shots > 0 && max_shots <= 65536, "bad arguments");
     *out = nullptr;
     w2d_batch* b = new w2d_batch();
+    b->device = current_device();
     b->max_shots = max_shots;
     auto fail = [&](int rc) {
         w2d_batch_destroy(b);
@@ -363,6 +365,7 @@ int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_sh
 
 void w2d_batch_destroy(w2d_batch* b)
 {
+    W2D_ON_DEVICE_OF(b);
     if (!b) return;
     if (b->st) cudaStreamSynchronize(b->st);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
@@ -384,6 +387,7 @@ void w2d_batch_destroy(w2d_batch* b)
 int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_per_launch,
                          int launches_per_graph)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b, "batch is NULL");
     W2D_CHECK_ARG((warps == 8 && rows_per_warp == 4) || (warps == 4 && rows_per_warp == 4) ||
                       (warps == 4 && rows_per_warp == 8) || (warps == 8 && rows_per_warp == 8),
@@ -412,6 +416,7 @@ int w2d_batch_set_config(w2d_batch* b, int warps, int rows_per_warp, int steps_p
 
 int w2d_batch_set_form(w2d_batch* b, int form)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b, "batch is NULL");
     W2D_CHECK_ARG(form == 0 || form == 1, "form must be 0 (queue) or 1 (grid)");
     W2D_CHECK_ARG(!b->in_flight, "change the form between replays only");
@@ -693,16 +698,19 @@ unsigned long long w2d_batch_model_bytes(const w2d_shot_desc* d) { return job_by
 
 int w2d_batch_submit(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
 {
+    W2D_ON_DEVICE_OF(b);
     return submit_job(b, d, 0, slot_out);
 }
 
 int w2d_batch_submit_modelling(w2d_batch* b, const w2d_shot_desc* d, int* slot_out)
 {
+    W2D_ON_DEVICE_OF(b);
     return submit_job(b, d, 1, slot_out);
 }
 
 int w2d_batch_launch(w2d_batch* b)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b, "batch is NULL");
     W2D_CHECK_ARG(!b->in_flight, "a replay is already in flight");
     b->last_ms = 0.f;
@@ -780,6 +788,7 @@ int w2d_batch_launch(w2d_batch* b)
 
 int w2d_batch_wait(w2d_batch* b, int* n_finished)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b, "batch is NULL");
     if (n_finished) *n_finished = 0;
     if (!b->in_flight) return W2D_OK;
@@ -825,6 +834,7 @@ int w2d_batch_wait(w2d_batch* b, int* n_finished)
 
 int w2d_batch_step(w2d_batch* b, int* n_finished)
 {
+    W2D_ON_DEVICE_OF(b);
     int rc;
     if ((rc = w2d_batch_launch(b))) return rc;
     return w2d_batch_wait(b, n_finished);
@@ -832,6 +842,7 @@ int w2d_batch_step(w2d_batch* b, int* n_finished)
 
 int w2d_batch_is_finished(w2d_batch* b, int slot)
 {
+    W2D_ON_DEVICE_OF(b);
     if (!b || slot < 0 || slot >= b->max_shots || !b->hs[slot].used) return -1;
     return b->hs[slot].finished ? 1 : 0;
 }
@@ -854,6 +865,7 @@ static void release_shot(w2d_batch* b, int slot)
 
 int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
     HostShot& h = b->hs[slot];
     W2D_CHECK_ARG(h.finished, "shot not finished");
@@ -874,6 +886,7 @@ int w2d_batch_fetch(w2d_batch* b, int slot, float* image_out, float* illum_out)
 
 int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
     HostShot& h = b->hs[slot];
     W2D_CHECK_ARG(h.finished, "shot not finished");
@@ -888,6 +901,7 @@ int w2d_batch_fetch_traces(w2d_batch* b, int slot, float* traces_out)
 
 int w2d_batch_cancel(w2d_batch* b, int slot)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b && slot >= 0 && slot < b->max_shots && b->hs[slot].used, "bad slot");
     W2D_CHECK_ARG(!b->in_flight, "cancel between replays only");
     auto it = std::find(b->active.begin(), b->active.end(), slot);
@@ -906,6 +920,7 @@ int w2d_batch_cancel(w2d_batch* b, int slot)
 int w2d_batch_stats(w2d_batch* b, int* n_active, float* last_ms, double* last_points,
                     long long* last_launches)
 {
+    W2D_ON_DEVICE_OF(b);
     W2D_CHECK_ARG(b, "batch is NULL");
     if (n_active) *n_active = (int)b->active.size();
     if (last_ms) *last_ms = b->last_ms;

@@ -28,6 +28,7 @@
 using namespace w2d;
 
 struct w2d_elastic {
+    int device = 0;  // CUDA device current at creation: every call on the handle runs there
     int nx = 0, nz = 0, ldx = 0, fs = 1;
     float dx = 0, dz = 0, dt = 0;
     size_t plane = 0;
@@ -200,6 +201,7 @@ int w2d_elastic_create(w2d_elastic** out, int nx, int nz, float dx, float dz, do
     W2D_CHECK_ARG(out && nx >= 5 && nz >= 5 && dx > 0 && dz > 0 && dt > 0, "bad arguments");
     *out = nullptr;
     w2d_elastic* e = new w2d_elastic();
+    e->device = current_device();
     e->nx = nx;
     e->nz = nz;
     e->ldx = pitch_for(nx);
@@ -234,6 +236,7 @@ int w2d_elastic_create(w2d_elastic** out, int nx, int nz, float dx, float dz, do
 
 void w2d_elastic_destroy(w2d_elastic* e)
 {
+    W2D_ON_DEVICE_OF(e);
     if (!e) return;
     if (e->st) cudaStreamSynchronize(e->st);
     for (void* p : {(void*)e->sponge, (void*)e->params, (void*)e->state, (void*)e->adj,
@@ -267,6 +270,7 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
                               const int* src_ix, const int* src_iz, const int* rec_ix, int n_rec,
                               int rec_iz, float* traces_dev)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && lam && mu && bx && bz && wavelets && traces_dev && nt > 0, "bad arguments");
     W2D_CHECK_ARG(n_shots >= 1 && n_shots <= 65535 && src_ix && src_iz, "bad shot count");
     W2D_CHECK_ARG(n_rec > 0 && rec_ix, "receivers required");
@@ -379,6 +383,7 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
                         const float* bz, const float* wavelet, int nt, int src_ix, int src_iz,
                         const int* rec_ix, int n_rec, int rec_iz, float* traces_dev)
 {
+    W2D_ON_DEVICE_OF(e);
     return w2d_elastic_forward_batch(e, 1, lam, mu, bx, bz, wavelet, nt, &src_ix, &src_iz, rec_ix,
                                      n_rec, rec_iz, traces_dev);
 }
@@ -388,6 +393,7 @@ int w2d_elastic_forward(w2d_elastic* e, const float* lam, const float* mu, const
 int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
                                float* g_bx, float* g_bz)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->have_forward && resid_dev, "call w2d_elastic_forward first");
     const int nt = e->nt, n_rec = e->n_rec, S = e->S;
     const size_t P = e->plane, pb = P * 4, SS = e->SS();
@@ -480,12 +486,14 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
 int w2d_elastic_gradient(w2d_elastic* e, const float* resid_dev, float* g_lam, float* g_mu,
                          float* g_bx, float* g_bz)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->S == 1, "the last forward call was a batch: use the batch gradient");
     return w2d_elastic_gradient_batch(e, resid_dev, g_lam, g_mu, g_bx, g_bz);
 }
 
 int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && (form == 0 || form == 1), "form must be 0 (per-cell) or 1 (tiled)");
     e->adj_form = form;
     return W2D_OK;
@@ -493,6 +501,7 @@ int w2d_elastic_set_adjoint(w2d_elastic* e, int form)
 
 int w2d_elastic_share_model(w2d_elastic* e, int on)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     e->shared_next = on ? 1 : 0;
     return W2D_OK;
@@ -500,6 +509,7 @@ int w2d_elastic_share_model(w2d_elastic* e, int on)
 
 int w2d_elastic_set_pdl(w2d_elastic* e, int on)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     e->pdl = on ? 1 : 0;
     return W2D_OK;
@@ -508,6 +518,7 @@ int w2d_elastic_set_pdl(w2d_elastic* e, int on)
 int w2d_elastic_set_tiles(w2d_elastic* e, int step_warps, int step_rows_per_warp,
                           int adjoint_warps, int adjoint_rows_per_warp)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     W2D_CHECK_ARG(el_tile_supported(step_warps, step_rows_per_warp),
                   "step tile must be 4x4, 4x2, 8x2 or 8x1 (warps x rows per warp)");

@@ -101,6 +101,7 @@ struct DevBuf {
 using namespace w2d;
 
 struct w2d_engine {
+    int device = 0;  // CUDA device current at creation: every call on the handle runs there
     int nx = 0, nz = 0, ldx = 0, fs = 1;
     float dx = 0, dz = 0, dt = 0;  // dt as the float the reference C code receives
     double dt_d = 0;               // dt as the Python float the reference drivers hold
@@ -540,6 +541,7 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
     W2D_CHECK_ARG(nx >= 5 && nz >= 5, "grid must be at least 5 x 5");
     W2D_CHECK_ARG(dx > 0 && dz > 0 && dt > 0, "dx, dz, dt must be positive");
     w2d_engine* e = new w2d_engine();
+    e->device = current_device();
     e->nx = nx;
     e->nz = nz;
     e->ldx = pitch_for(nx);
@@ -641,6 +643,7 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
 
 void w2d_engine_destroy(w2d_engine* e)
 {
+    W2D_ON_DEVICE_OF(e);
     if (!e) return;
     if (e->stream) cudaStreamSynchronize(e->stream);
     for (DevBuf<float>* b : {&e->sponge_lut, &e->sponge_arr, &e->waves, &e->v2dt2, &e->staging,
@@ -669,6 +672,7 @@ void w2d_engine_destroy(w2d_engine* e)
 
 int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     if (warps == 0 && rows_per_warp == 0) {
         warps = 4;
@@ -681,6 +685,7 @@ int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp)
 
 int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
     e->persistent = persistent ? 1 : 0;
@@ -690,6 +695,7 @@ int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
 
 int w2d_engine_set_two_step(w2d_engine* e, int rows_per_warp)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     W2D_CHECK_ARG(rows_per_warp == 0 || rows_per_warp == 1 ||
                       (rows_per_warp >= 2 && rows_per_warp <= 4),
@@ -701,6 +707,7 @@ int w2d_engine_set_two_step(w2d_engine* e, int rows_per_warp)
 
 int w2d_engine_set_l2_hints(w2d_engine* e, int on)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     e->l2_hints = on ? 1 : 0;
     return W2D_OK;
@@ -708,6 +715,7 @@ int w2d_engine_set_l2_hints(w2d_engine* e, int on)
 
 int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     e->budget = bytes;
     return W2D_OK;
@@ -715,6 +723,7 @@ int w2d_engine_set_memory_budget(w2d_engine* e, unsigned long long bytes)
 
 int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && vel, "NULL argument");
     W2D_CHECK_ARG(slot == 0 || slot == 1, "velocity slot must be 0 or 1");
     int rc;
@@ -732,6 +741,7 @@ int w2d_forward(w2d_engine* e, int vel_slot, const float* wavelet, int nt, int s
                 const int* rec_ix, int n_rec, int rec_iz, float* rec_out, float* snaps_out,
                 int snapshot_interval)
 {
+    W2D_ON_DEVICE_OF(e);
     int rc;
     if ((rc = common_checks(e, nt, snapshot_interval))) return rc;
     W2D_CHECK_ARG(vel_slot == 0 || vel_slot == 1, "bad velocity slot");
@@ -784,6 +794,7 @@ int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int n
                            const int* rec_ix, int n_rec, int rec_iz, const float* fwd_snaps,
                            int n_snaps, float* image, int snapshot_interval)
 {
+    W2D_ON_DEVICE_OF(e);
     int rc;
     if ((rc = common_checks(e, nt, snapshot_interval))) return rc;
     W2D_CHECK_ARG(vel_slot == 0 || vel_slot == 1, "bad velocity slot");
@@ -980,6 +991,7 @@ int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, in
                      const float* data, const int* rec_ix, int n_rec, int rec_iz,
                      int snapshot_interval, int storage, float* image_out, float* illum_out)
 {
+    W2D_ON_DEVICE_OF(e);
     int rc;
     if ((rc = migrate_checks(e, nt, snapshot_interval, src_ix, src_iz, n_rec, image_out,
                              illum_out)))
@@ -1014,6 +1026,7 @@ int w2d_migrate_shot(w2d_engine* e, const float* wavelet, int nt, int src_ix, in
 int w2d_shot_stage(w2d_engine* e, int slot, const float* wavelet, int nt, const float* data,
                    int n_rec)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && wavelet && nt > 0 && slot >= 0 && slot < 4096, "bad arguments");
     W2D_CHECK_ARG(n_rec >= 0 && (n_rec == 0 || data), "bad data");
     if ((int)e->st_w.size() <= slot) {
@@ -1041,6 +1054,7 @@ int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const in
                        int n_rec, int rec_iz, int snapshot_interval, int storage,
                        float* image_out, float* illum_out)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && slot >= 0 && slot < (int)e->st_nt.size() && e->st_nt[slot] > 0,
                   "slot not staged");
     W2D_CHECK_ARG(n_rec == e->st_nrec[slot], "n_rec differs from the staged data");
@@ -1057,6 +1071,7 @@ int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const in
 
 int w2d_engine_timer_start(w2d_engine* e)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     if (!e->t0 && (cudaEventCreate(&e->t0) != cudaSuccess || cudaEventCreate(&e->t1) != cudaSuccess)) {
         set_error("event creation failed");
@@ -1068,6 +1083,7 @@ int w2d_engine_timer_start(w2d_engine* e)
 
 int w2d_engine_timer_stop(w2d_engine* e, float* ms)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->t0 && ms, "timer not started");
     W2D_CUDA_TRY(cudaEventRecord(e->t1, e->stream));
     W2D_CUDA_TRY(cudaEventSynchronize(e->t1));
@@ -1099,6 +1115,7 @@ int w2d_device_memory(unsigned long long* free_bytes, unsigned long long* total_
 
 int w2d_stack_reset(w2d_engine* e)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     int rc;
     if ((rc = e->stack_img.ensure(e->plane)) || (rc = e->stack_ill.ensure(e->plane))) return rc;
@@ -1110,6 +1127,7 @@ int w2d_stack_reset(w2d_engine* e)
 
 int w2d_stack_add(w2d_engine* e, const float* image, const float* illum)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && image && illum, "NULL argument");
     W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
     int rc;
@@ -1125,6 +1143,7 @@ int w2d_stack_add(w2d_engine* e, const float* image, const float* illum)
 
 int w2d_stack_read(w2d_engine* e, float* image_out, float* illum_out)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && image_out && illum_out, "NULL argument");
     W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
     int rc;
@@ -1212,6 +1231,7 @@ extern "C" {
 int w2d_post_stack(w2d_engine* e, int mute_sponge, float* raw_out, float* laplacian_out,
                    float* normalized_out)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && raw_out && laplacian_out && normalized_out, "NULL argument");
     W2D_CHECK_ARG(e->stack_img.p, "stack is empty (call w2d_stack_reset first)");
     int rc;
@@ -1304,6 +1324,7 @@ extern "C" {
 int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, int nt, int src_ix,
                     int src_iz, const int* rec_ix, int n_rec, int rec_iz, float* traces_dev)
 {
+    W2D_ON_DEVICE_OF(e);
     int rc;
     if ((rc = common_checks(e, nt, 1))) return rc;
     W2D_CHECK_ARG(vel_dev && wavelet && traces_dev, "NULL argument");
@@ -1354,6 +1375,7 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
 
 int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->fwi && e->fwi->nt > 0, "call w2d_fwi_forward first");
     W2D_CHECK_ARG(resid_dev && grad_dev, "NULL argument");
     w2d_fwi_state* f = e->fwi;
@@ -1421,6 +1443,7 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
 
 int w2d_engine_synchronize(w2d_engine* e)
 {
+    W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
     return W2D_OK;

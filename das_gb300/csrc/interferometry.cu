@@ -331,6 +331,7 @@ int scratch_stream()
 }  // namespace
 
 struct w2d_xcorr {
+    int device = 0;  // CUDA device current at creation: every call on the handle runs there
     int nt = 0, n_ch = 0, n_src = 0, n_rec = 0, lag0 = 0, n_rows = 0, pad = 0, n_added = 0;
     int n_lags = 0;
     size_t r_rows = 0;  // rows of the zero-padded receiver buffer
@@ -377,6 +378,7 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
         W2D_CHECK_ARG(rec_ch[i] >= 0 && rec_ch[i] < n_ch, "receiver channel out of range");
     *out = nullptr;
     w2d_xcorr* x = new w2d_xcorr();
+    x->device = current_device();
     x->nt = nt;
     x->n_ch = n_ch;
     x->n_src = n_src;
@@ -425,6 +427,7 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
 
 void w2d_xcorr_destroy(w2d_xcorr* x)
 {
+    W2D_ON_DEVICE_OF(x);
     if (!x) return;
     if (x->st) cudaStreamSynchronize(x->st);
     if (x->st_copy) cudaStreamSynchronize(x->st_copy);
@@ -448,6 +451,7 @@ int w2d_xcorr_shape(w2d_xcorr* x, int* lag0, int* n_rows)
 
 int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt)
 {
+    W2D_ON_DEVICE_OF(x);
     W2D_CHECK_ARG(x && data_dev, "NULL argument");
     W2D_CHECK_ARG(nt >= 1 && nt <= x->nt, "window longer than the stack was created for");
     int lag0 = 0, n_rows = 0;
@@ -480,6 +484,7 @@ int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt)
 // once); the correlation of the previous window keeps running meanwhile.
 int w2d_xcorr_add(w2d_xcorr* x, const float* data_host, int nt)
 {
+    W2D_ON_DEVICE_OF(x);
     W2D_CHECK_ARG(x && data_host, "NULL argument");
     W2D_CHECK_ARG(nt >= 1 && nt <= x->nt, "window longer than the stack was created for");
     const int b = x->n_added & 1;
@@ -495,6 +500,7 @@ int w2d_xcorr_add(w2d_xcorr* x, const float* data_host, int nt)
 
 int w2d_xcorr_read(w2d_xcorr* x, float* out_host, int divide)
 {
+    W2D_ON_DEVICE_OF(x);
     W2D_CHECK_ARG(x && out_host, "NULL argument");
     W2D_CHECK_ARG(x->n_added > 0, "no window added");
     const size_t n = (size_t)x->n_src * x->n_rows * x->n_rec;

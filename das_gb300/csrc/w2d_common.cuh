@@ -40,6 +40,41 @@ const char* last_error();
         }                                                                              \
     } while (0)
 
+// Makes `device` the calling thread's current device for the scope of one entry point
+// and restores the caller's device at its end.  Every handle (engine, batch, elastic
+// engine, correlation stack) records the device current when it was created; the
+// device is per host thread, so a handle made on one device and called from another
+// thread, or after w2d_set_device chose another device, still runs on its own.
+// device < 0 (a NULL handle) does nothing: the entry point reports the bad handle.
+class DeviceScope {
+  public:
+    explicit DeviceScope(int device)
+    {
+        int cur = -1;
+        if (device >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != device &&
+            cudaSetDevice(device) == cudaSuccess)
+            prev_ = cur;
+    }
+    ~DeviceScope()
+    {
+        if (prev_ >= 0) cudaSetDevice(prev_);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+
+  private:
+    int prev_ = -1;
+};
+
+// The device current on the calling thread (0 when none can be read).
+inline int current_device()
+{
+    int d = 0;
+    return cudaGetDevice(&d) == cudaSuccess ? d : 0;
+}
+
+#define W2D_ON_DEVICE_OF(h) ::w2d::DeviceScope _w2d_device_scope((h) ? (h)->device : -1)
+
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 inline int pitch_for(int nx) { return round_up(nx, 32); }
 

@@ -166,6 +166,9 @@ class ElasticExecutor:
         self._jobs = {}  # job_id -> [request, results, shots left]
         self._solvers = {}
         self.budget = int(budget_gb * (1 << 30))  # device bytes per worker for one batch
+        # the creating thread's device: the CUDA device is per host thread and a new
+        # thread starts on device 0, so each worker selects this one before any CUDA call
+        self._device = torch.cuda.current_device() if torch.cuda.is_available() else None
         self._threads = [threading.Thread(target=self._loop, daemon=True)
                          for _ in range(max(1, int(workers)))]
         for t in self._threads:
@@ -228,6 +231,9 @@ class ElasticExecutor:
 
     def _loop(self):
         import time
+        if self._device is not None:
+            torch.cuda.set_device(self._device)
+            _lib.check(_lib.load().w2d_set_device(self._device))
         torch.cuda.set_stream(torch.cuda.Stream())
         key, solver = None, None
         while True:

@@ -162,7 +162,10 @@ int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const in
 int w2d_engine_timer_start(w2d_engine* e);
 int w2d_engine_timer_stop(w2d_engine* e, float* ms);
 
-/* Select the CUDA device used by engines created afterwards on this host thread. */
+/* Select the CUDA device used by engines created afterwards on this host thread.
+ * Every handle (engine, batch, elastic engine, correlation stack) keeps the device
+ * that was current when it was created: calls on it run there, from any host thread,
+ * and leave the calling thread's current device as they found it. */
 int w2d_set_device(int device);
 /* PCI bus id ("0000:xx:00.0") of the current device, for per-GPU monitoring. */
 int w2d_device_pci_bus_id(char* buf, int len);
