@@ -274,6 +274,11 @@ int w2d_elastic_forward_batch(w2d_elastic* e, int n_shots, const float* lam, con
     W2D_CHECK_ARG(e && lam && mu && bx && bz && wavelets && traces_dev && nt > 0, "bad arguments");
     W2D_CHECK_ARG(n_shots >= 1 && n_shots <= 65535 && src_ix && src_iz, "bad shot count");
     W2D_CHECK_ARG(n_rec > 0 && rec_ix, "receivers required");
+    W2D_CHECK_DEVICE_PTR(lam, e->device);
+    W2D_CHECK_DEVICE_PTR(mu, e->device);
+    W2D_CHECK_DEVICE_PTR(bx, e->device);
+    W2D_CHECK_DEVICE_PTR(bz, e->device);
+    W2D_CHECK_DEVICE_PTR(traces_dev, e->device);
     for (int s = 0; s < n_shots; ++s)
         W2D_CHECK_ARG(src_ix[s] >= 0 && src_ix[s] < e->nx && src_iz[s] >= 0 && src_iz[s] < e->nz &&
                           on_m(e, src_iz[s], src_ix[s]),
@@ -395,6 +400,11 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
 {
     W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->have_forward && resid_dev, "call w2d_elastic_forward first");
+    W2D_CHECK_DEVICE_PTR(resid_dev, e->device);
+    W2D_CHECK_DEVICE_PTR(g_lam, e->device);
+    W2D_CHECK_DEVICE_PTR(g_mu, e->device);
+    W2D_CHECK_DEVICE_PTR(g_bx, e->device);
+    W2D_CHECK_DEVICE_PTR(g_bz, e->device);
     const int nt = e->nt, n_rec = e->n_rec, S = e->S;
     const size_t P = e->plane, pb = P * 4, SS = e->SS();
     const size_t tr_stride = (size_t)nt * n_rec;

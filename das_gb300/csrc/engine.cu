@@ -1328,6 +1328,8 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
     int rc;
     if ((rc = common_checks(e, nt, 1))) return rc;
     W2D_CHECK_ARG(vel_dev && wavelet && traces_dev, "NULL argument");
+    W2D_CHECK_DEVICE_PTR(vel_dev, e->device);
+    W2D_CHECK_DEVICE_PTR(traces_dev, e->device);
     W2D_CHECK_ARG(n_rec > 0 && rec_ix, "receivers required");
     W2D_CHECK_ARG(e->tile.rpw == 4 && (e->tile.warps == 4 || e->tile.warps == 8),
                   "the adjoint path runs with 4x4 or 8x4 tiles");
@@ -1378,6 +1380,8 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
     W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e && e->fwi && e->fwi->nt > 0, "call w2d_fwi_forward first");
     W2D_CHECK_ARG(resid_dev && grad_dev, "NULL argument");
+    W2D_CHECK_DEVICE_PTR(resid_dev, e->device);
+    W2D_CHECK_DEVICE_PTR(grad_dev, e->device);
     w2d_fwi_state* f = e->fwi;
     const int nt = f->nt, n_rec = f->n_rec, seg = f->seg;
     const size_t plane_b = e->plane * 4;

@@ -453,6 +453,7 @@ int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt)
 {
     W2D_ON_DEVICE_OF(x);
     W2D_CHECK_ARG(x && data_dev, "NULL argument");
+    W2D_CHECK_DEVICE_PTR(data_dev, x->device);
     W2D_CHECK_ARG(nt >= 1 && nt <= x->nt, "window longer than the stack was created for");
     int lag0 = 0, n_rows = 0;
     w2d_xcorr_rows(nt, x->n_lags, &lag0, &n_rows);

@@ -75,6 +75,37 @@ inline int current_device()
 
 #define W2D_ON_DEVICE_OF(h) ::w2d::DeviceScope _w2d_device_scope((h) ? (h)->device : -1)
 
+// A caller's DEVICE pointer must be device (or managed) memory of the handle's device: a
+// host pointer, or memory of another GPU, is refused here with W2D_EINVAL instead of
+// reaching a kernel.  NULL passes (the entry points check NULL themselves).
+inline int check_device_ptr(const void* p, int device, const char* what)
+{
+    if (!p) return W2D_OK;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // the query's error is not sticky: clear it for later checks
+        set_error(std::string(what) + " is not a CUDA pointer");
+        return W2D_EINVAL;
+    }
+    if (a.type == cudaMemoryTypeManaged) return W2D_OK;
+    if (a.type != cudaMemoryTypeDevice) {
+        set_error(std::string(what) + " is not device memory");
+        return W2D_EINVAL;
+    }
+    if (a.device != device) {
+        set_error(std::string(what) + " is on device " + std::to_string(a.device) +
+                  ", the handle on device " + std::to_string(device));
+        return W2D_EINVAL;
+    }
+    return W2D_OK;
+}
+
+#define W2D_CHECK_DEVICE_PTR(p, dev)                                                   \
+    do {                                                                               \
+        const int _rc = ::w2d::check_device_ptr((p), (dev), #p);                       \
+        if (_rc) return _rc;                                                           \
+    } while (0)
+
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 inline int pitch_for(int nx) { return round_up(nx, 32); }
 

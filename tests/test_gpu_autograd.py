@@ -103,3 +103,53 @@ def test_gradient_of_8000_steps_on_the_large_grid():
     assert np.isfinite(J) and J > 0
     assert np.isfinite(g).all() and np.abs(g).max() > 0
     s.close()
+
+
+def test_device_arguments_refuse_host_memory():
+    """A DEVICE argument that is host memory is refused on the host with W2D_EINVAL
+    before any launch, and the handle stays usable.  The host memory is page-locked,
+    which the device can read through its mapping, so no launch could fault on it even
+    if the check let it through."""
+    import torch
+    from das_gb300 import _lib
+    from das_gb300.elastic import ElasticSolver2D
+    from das_gb300.pinned import pinned_array
+    s, grid, v0, vt, w, rix, d_obs, _ = _setup()
+    lib = _lib.load()
+    w32 = np.ascontiguousarray(w, dtype=np.float32)
+    r = np.ascontiguousarray(rix, dtype=np.int32)
+    host_vel = pinned_array(v0.shape)
+    host_vel[...] = v0
+    traces = torch.empty((len(w32), len(r)), dtype=torch.float32, device="cuda")
+
+    def msg():
+        m = lib.w2d_last_error()
+        return m.decode() if isinstance(m, bytes) else str(m)
+
+    rc = lib.w2d_fwi_forward(s._eng(), host_vel.ctypes.data, w32.ctypes.data, len(w32), 50, 6,
+                             r.ctypes.data, len(r), 3, traces.data_ptr())
+    assert rc == 1 and "not device memory" in msg(), msg()
+    vel = torch.tensor(v0, device="cuda")
+    torch.cuda.synchronize()
+    assert lib.w2d_fwi_forward(s._eng(), vel.data_ptr(), w32.ctypes.data, len(w32), 50, 6,
+                               r.ctypes.data, len(r), 3, traces.data_ptr()) == 0
+    torch.cuda.synchronize()
+    d_ref, _ = s.forward_propagate_acoustic(v0, w, 50, 6, rix, 3)
+    np.testing.assert_array_equal(traces.cpu().numpy(), d_ref)
+
+    es = ElasticSolver2D(64, 32, 2.0, 2.0, 2e-4, 8, 0.0015, True)
+    try:
+        lam = pinned_array((32, 64))
+        lam[...] = 1.0
+        dev = torch.ones((32, 64), dtype=torch.float32, device="cuda")
+        etr = torch.empty((1, 20, 60), dtype=torch.float32, device="cuda")
+        ew = np.zeros((1, 20), np.float32)
+        six, siz = np.array([32], np.int32), np.array([10], np.int32)
+        erix = np.arange(2, 62, dtype=np.int32)
+        rc = lib.w2d_elastic_forward_batch(es._h, 1, lam.ctypes.data, dev.data_ptr(),
+                                           dev.data_ptr(), dev.data_ptr(), ew.ctypes.data, 20,
+                                           six.ctypes.data, siz.ctypes.data, erix.ctypes.data,
+                                           len(erix), 2, etr.data_ptr())
+        assert rc == 1 and "lam" in msg() and "not device memory" in msg(), msg()
+    finally:
+        es.close()
