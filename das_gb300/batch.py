@@ -229,6 +229,12 @@ class BatchEngine:
     def finished(self, slot: int) -> bool:
         return self._lib.w2d_batch_is_finished(self._h, int(slot)) == 1
 
+    def cancel(self, slot: int) -> None:
+        """Drop an admitted job, running or finished, between replays (no replay in
+        flight): its device memory returns to the arena, its slot is free again, and the
+        other jobs continue with results unchanged."""
+        _lib.check(self._lib.w2d_batch_cancel(self._h, int(slot)))
+
     def fetch(self, slot: int, nz: int, nx: int) -> Tuple[np.ndarray, np.ndarray]:
         img = np.empty((nz, nx), np.float32)
         ill = np.empty((nz, nx), np.float32)

@@ -210,3 +210,35 @@ def test_batch_shot_without_receivers_and_one_step():
         np.testing.assert_array_equal(ill, ref_ill)
     assert not results[1][0].any()
     eng.close()
+
+
+def test_cancel_mid_run_leaves_the_others_unchanged():
+    """A job cancelled between replays leaves the batch: its slot is free again, its
+    memory returns to the arena, and the jobs still running finish with the results they
+    have alone."""
+    from das_gb300.batch import BatchEngine
+    jobs = [_job(40, 50, 180, 150), _job(41, 60, 220, 170), _job(42, 45, 150, 130)]
+    eng = BatchEngine(arena_bytes=1 << 28, max_shots=4, steps_per_launch=8, launches_per_graph=2)
+    free0 = eng.free_bytes()
+    slots = [eng.submit(j) for j in jobs]
+    assert None not in slots
+    eng.step()  # 16 phase steps of every job: all still running
+    assert not any(eng.finished(s) for s in slots)
+    eng.cancel(slots[1])
+    assert eng._lib.w2d_batch_is_finished(eng._h, slots[1]) == -1
+    left = {slots[0]: jobs[0], slots[2]: jobs[2]}
+    out = {}
+    for _ in range(1000):
+        if len(out) == len(left):
+            break
+        eng.step()
+        for s, j in left.items():
+            if s not in out and eng.finished(s):
+                out[s] = eng.fetch(s, j.nz, j.nx)
+    assert len(out) == len(left)
+    assert eng.free_bytes() == free0
+    for s, j in left.items():
+        ref_img, ref_ill = _alone(j)
+        np.testing.assert_array_equal(out[s][0], ref_img)
+        np.testing.assert_array_equal(out[s][1], ref_ill)
+    eng.close()
