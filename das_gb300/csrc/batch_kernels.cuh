@@ -220,13 +220,12 @@ struct BatchStepArgs {
     unsigned* err;
 };
 
-// (4-row tiles are held to 64 registers so that 8 CTAs of 4 warps fit an SM: the shared
-// memory of a 128 x 16 tile allows it.)
 // Grid form: one launch advances every active shot by one phase step, one CTA
 // per (shot, tile); the launches after the first of a replay are programmatic
 // dependents of the one before, so a launch's set-up overlaps the previous one's
 // last wave (the first waits normally for the active-list copies and admission
-// events before it).  No waits between CTAs.
+// events before it).  No waits between CTAs.  4-row tiles are held to 64 registers
+// so that 8 CTAs of 4 warps fit an SM (the shared memory of a 128 x 16 tile allows it).
 template <int WARPS, int RPW>
 __global__ void __launch_bounds__(WARPS * 32, RPW <= 4 ? 1024 / (WARPS * 32) : 1)
     acoustic_batch_step_kernel(const BatchStepArgs a)
