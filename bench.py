@@ -916,7 +916,9 @@ def main():
     rank, world, local = dist_env()
     if world > 1:
         import torch
+        from das_gb300 import _lib
         torch.cuda.set_device(local)
+        _lib.check(_lib.load().w2d_set_device(local))  # handles made on this thread bind here
     dist = Dist("nccl" if world > 1 else "gloo")
     try:
         if args.workload == "batched":
