@@ -17,7 +17,7 @@ import json
 import os
 import time
 from dataclasses import replace
-from typing import List, Optional, Sequence, Tuple
+from typing import List, Sequence, Tuple
 
 import numpy as np
 

@@ -25,7 +25,7 @@ import ctypes
 import os
 import subprocess
 from dataclasses import dataclass
-from typing import List, Optional, Sequence, Tuple
+from typing import Optional, Sequence, Tuple
 
 import numpy as np
 
