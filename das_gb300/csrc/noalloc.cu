@@ -9,17 +9,28 @@
 // scratch buffer it needs -- three wavefield planes, the vel^2 dt^2 plane, the
 // receiver table, the sponge table, the source/receiver rows and an error word --
 // in ONE file-scope __device__ array of fixed size (W2D_NOALLOC_SCRATCH_BYTES).
-// Every GPU that loads this library holds that array until the process exits.
+//
+// When the array occupies device memory: with the CUDA runtime's default lazy
+// module loading the module holding the array is loaded on a device at the first
+// launch or symbol lookup there, so the array is mapped by the first call of this
+// entry point on that device (or when the library is loaded, under
+// CUDA_MODULE_LOADING=EAGER) and stays until the process exits.  A caller that
+// needs a fixed footprint makes one warm-up call per device before the region it
+// measures.  That first call can fail with W2D_ECUDA (out of memory) if the
+// device has no room for the array.
 //
 // Host code must not use the array's name as a device address: on the host the
-// name is only a stand-in.  At its first call on a device (with that device
+// name is only a stand-in.  At the first call on a device (with that device
 // current) the entry point asks the runtime for the array's device address with
-// cudaGetSymbolAddress and caches it per device; that first call should come
-// before any stream capture.  All calls share the array and it keeps the last
-// call's contents: each call clears the wavefield planes and the error word it
-// relies on.  Calls whose work overlaps on the GPU (two host threads, or two
-// streams) race on the array; the entry point serialises host callers with a
-// mutex and finishes its work (stream synchronise) before returning.
+// cudaGetSymbolAddress and caches it per device id; that first call should come
+// before any stream capture.  cudaDeviceReset invalidates the cached address and
+// is not supported between calls.  Each call is synchronous: it waits for its
+// copies and kernels with cudaStreamSynchronize, on error paths too.  All calls
+// share the array and it keeps the last call's contents: each call clears the
+// wavefield planes and the error word it relies on.  Calls whose work overlaps on
+// the GPU (two host threads, or two streams) would race on the array; the entry
+// point serialises host callers with a mutex and finishes its work before
+// returning.
 #include <string.h>
 
 #include <mutex>
@@ -105,6 +116,10 @@ int w2d_forward_noalloc(const float* vel_dev, const float* wavelet_dev, int nt, 
     int dev = 0;
     W2D_CUDA_TRY(cudaGetDevice(&dev));
     W2D_CHECK_ARG(dev >= 0 && dev < 64, "device id out of range");
+    // the caller's buffers must be device memory of the current device
+    W2D_CHECK_DEVICE_PTR(vel_dev, dev);
+    W2D_CHECK_DEVICE_PTR(wavelet_dev, dev);
+    W2D_CHECK_DEVICE_PTR(traces_dev, dev);
     if (!g_addr[dev]) {
         // once per device, with that device current: the array's device address
         void* p = nullptr;
@@ -133,14 +148,35 @@ int w2d_forward_noalloc(const float* vel_dev, const float* wavelet_dev, int nt, 
     for (int d = 1; d <= n_lut; ++d) g_lut[d] = cerjan_value(d, sponge_alpha);
     const int sh[4] = {src_ix, src_iz, rec_iz, n_rec};
 
-    W2D_CUDA_TRY(cudaMemsetAsync(wave, 0, 3 * plane * 4, st));
-    W2D_CUDA_TRY(cudaMemsetAsync(err, 0, 4, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(rptr, g_ptr, (nx + 1) * 4, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(rlist, g_list, n_rec * 4, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(lut, g_lut, (n_lut + 1) * 4, cudaMemcpyHostToDevice, st));
-    W2D_CUDA_TRY(cudaMemcpyAsync(shot, sh, sizeof sh, cudaMemcpyHostToDevice, st));
+    // tensor maps are host-side encodings of the scratch planes: build them before any
+    // work is queued, so that a failure here leaves nothing running
+    AcMaps maps[3];
+    for (int i = 0; i < 3; ++i) {
+        const int rc = make_ac_maps(&maps[i], wave + (size_t)((i + 1) % 3) * plane,
+                                    wave + (size_t)i * plane, vel, nullptr, nx, nz, ldx, 16);
+        if (rc) return rc;
+    }
+
+    // From here on work is queued on st.  Every failure waits for what is already
+    // queued before returning, so that no kernel of this call still writes the shared
+    // scratch when the next call (perhaps on another stream) starts.
+#define NA_TRY(expr)                                                                   \
+    do {                                                                               \
+        cudaError_t _e = (expr);                                                       \
+        if (_e != cudaSuccess) {                                                       \
+            set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));             \
+            cudaStreamSynchronize(st);                                                 \
+            return W2D_ECUDA;                                                          \
+        }                                                                              \
+    } while (0)
+    NA_TRY(cudaMemsetAsync(wave, 0, 3 * plane * 4, st));
+    NA_TRY(cudaMemsetAsync(err, 0, 4, st));
+    NA_TRY(cudaMemcpyAsync(rptr, g_ptr, (nx + 1) * 4, cudaMemcpyHostToDevice, st));
+    NA_TRY(cudaMemcpyAsync(rlist, g_list, n_rec * 4, cudaMemcpyHostToDevice, st));
+    NA_TRY(cudaMemcpyAsync(lut, g_lut, (n_lut + 1) * 4, cudaMemcpyHostToDevice, st));
+    NA_TRY(cudaMemcpyAsync(shot, sh, sizeof sh, cudaMemcpyHostToDevice, st));
     // the host tables are reused by the next call: finish the copies first
-    W2D_CUDA_TRY(cudaStreamSynchronize(st));
+    NA_TRY(cudaStreamSynchronize(st));
 
     const float dtf = (float)dt;
     noalloc_model_kernel<<<grid_for(plane), 256, 0, st>>>(vel, vel_dev, nx, nz, ldx, dtf * dtf);
@@ -159,13 +195,7 @@ int w2d_forward_noalloc(const float* vel_dev, const float* wavelet_dev, int nt, 
     g.shot = shot;
     const float dt2inj = (float)(dt * dt);
     inject_kernel<<<(nx + 255) / 256, 256, 0, st>>>(wave + plane, g, wavelet_dev, nullptr, dt2inj);
-    W2D_CUDA_TRY(cudaGetLastError());
-    AcMaps maps[3];
-    int rc;
-    for (int i = 0; i < 3; ++i)
-        if ((rc = make_ac_maps(&maps[i], wave + (size_t)((i + 1) % 3) * plane,
-                               wave + (size_t)i * plane, vel, nullptr, nx, nz, ldx, 16)))
-            return rc;
+    NA_TRY(cudaGetLastError());
     for (int it = 0; it < nt; ++it) {
         AcStep s;
         memset(&s, 0, sizeof s);
@@ -175,11 +205,12 @@ int w2d_forward_noalloc(const float* vel_dev, const float* wavelet_dev, int nt, 
         s.dt2_inj = dt2inj;
         s.err = err;
         // maps[i]: p_curr = plane (i+1)%3, p_prev = plane i, for it % 3 == i
-        W2D_CUDA_TRY((launch_acoustic_step<4, 4, SPONGE_LUT>(maps[it % 3], g, s, st)));
+        NA_TRY((launch_acoustic_step<4, 4, SPONGE_LUT>(maps[it % 3], g, s, st)));
     }
     unsigned h = 0;
-    W2D_CUDA_TRY(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st));
-    W2D_CUDA_TRY(cudaStreamSynchronize(st));
+    NA_TRY(cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st));
+    NA_TRY(cudaStreamSynchronize(st));
+#undef NA_TRY
     if (h) {
         set_error("device wait gave up in w2d_forward_noalloc");
         return W2D_ETIMEOUT;

@@ -14,12 +14,23 @@
  * Limits: at most W2D_NOALLOC_MAX_POINTS pitched cells per field (pitch = nx
  * rounded up to 32), W2D_NOALLOC_MAX_NX columns, W2D_NOALLOC_MAX_RECEIVERS
  * receivers, W2D_NOALLOC_MAX_SPONGE sponge cells; larger requests return
- * W2D_EINVAL with a message.  The first call on a device, made with that device
- * current, looks up the scratch array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  Calls share the scratch and
- * it keeps the last call's contents; every call clears what it relies on.
- * Calls whose GPU work overlaps (other threads or streams) race on the scratch:
- * host callers are serialised and each call finishes its work before returning.
+ * W2D_EINVAL with a message.
+ *
+ * The scratch array is mapped on a device when the library's module is loaded
+ * there: at the first call on that device under the runtime's default lazy
+ * module loading (or at library load with CUDA_MODULE_LOADING=EAGER).  That
+ * first call, made with the device current, also looks up the array's device
+ * address (cudaGetSymbolAddress) and caches it per device id; a caller that
+ * needs a fixed device footprint makes it once as a warm-up, outside the
+ * region it measures, and before any stream capture.  cudaDeviceReset between
+ * calls is not supported (the cached address would be stale).  Every call is
+ * synchronous: it waits for its own work before returning, on error paths
+ * too.  Calls share the scratch and it keeps the last call's
+ * contents; every call clears what it relies on.  Calls whose GPU work would
+ * overlap (other threads or streams) would race on the scratch: host callers
+ * are serialised by a mutex and each call finishes its work before returning.
+ * vel_dev, wavelet_dev and traces_dev must be device memory of the current
+ * device; host memory or another GPU's memory is refused with W2D_EINVAL.
  */
 #ifndef WAVE2D_NOALLOC_H
 #define WAVE2D_NOALLOC_H
@@ -34,9 +45,10 @@ extern "C" {
 #define W2D_NOALLOC_MAX_SPONGE 1024
 #define W2D_NOALLOC_SCRATCH_BYTES (4u * (4u * W2D_NOALLOC_MAX_POINTS + 16384u))
 
-/* Forward modelling (forward_propagate_acoustic, wave_solver.py:128-186, without
- * snapshots) in velocity vel_dev (DEVICE, contiguous nz x nx) with the Cerjan
- * sponge (n_sponge, sponge_alpha) the solver would build; wavelet_dev (DEVICE,
+/* Forward modelling without snapshots -- the same traces this library's
+ * w2d_forward returns for the same arguments -- in velocity vel_dev (DEVICE,
+ * contiguous nz x nx) with the Cerjan sponge (n_sponge, sponge_alpha) the
+ * solver would build; wavelet_dev (DEVICE,
  * nt); receiver columns rec_ix (HOST, n_rec); traces_dev (DEVICE, nt x n_rec)
  * receives the traces.  stream: a cudaStream_t, or NULL for the default stream.
  * Synchronous.  Returns W2D_OK or a W2D_E* code (w2d_last_error()). */

@@ -23,8 +23,9 @@ import types
 
 import numpy as np
 
-REF_ROOT = os.environ.get("DAS_REFERENCE_ROOT", "/root/reference")
 REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+# the reference checkout: DAS_REFERENCE_ROOT, else a sibling folder "reference" beside the repo
+REF_ROOT = os.environ.get("DAS_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference"))
 OUT = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(REPO, "oracle", "_ref", "libwave2d.so")
 

@@ -26,8 +26,10 @@ import numpy as np
 from scipy.interpolate import interp1d
 from scipy.ndimage import gaussian_filter1d
 
-REF_ROOT = os.environ.get("DAS_REFERENCE_ROOT", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(OUT))
+# the reference checkout: DAS_REFERENCE_ROOT, else a sibling folder "reference" beside the repo
+REF_ROOT = os.environ.get("DAS_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference"))
 
 
 def load_interferometry():

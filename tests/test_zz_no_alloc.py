@@ -71,3 +71,27 @@ def test_no_alloc_rejects_oversized_grids():
     rc = fn(v_d.data_ptr(), w_d.data_ptr(), 8, nx, nz, 5.0, 5.0, 1e-4, 10, 0.0015, 1, 10, 2,
             rix.ctypes.data, 4, 2, out_d.data_ptr(), None)
     assert rc == 1 and b"scratch" in lib.w2d_last_error()
+
+
+def test_no_alloc_refuses_host_memory():
+    """A DEVICE argument that is host memory is refused with W2D_EINVAL before any
+    work is queued.  The host buffer is page-locked, which the device could read
+    through its mapping, so nothing could fault even if the check let it through;
+    a following call with device buffers still succeeds."""
+    import torch
+    from das_gb300.pinned import pinned_array
+    lib, fn = _bind()
+    nz, nx, nt = 40, 64, 16
+    host_vel = pinned_array((nz, nx))
+    host_vel[...] = 2000.0
+    w_d = torch.zeros(nt, device="cuda")
+    out_d = torch.zeros((nt, 4), device="cuda")
+    v_d = torch.full((nz, nx), 2000.0, device="cuda")
+    rix = np.arange(4, dtype=np.int32)
+    torch.cuda.synchronize()
+    rc = fn(host_vel.ctypes.data, w_d.data_ptr(), nt, nx, nz, 5.0, 5.0, 5e-4, 10, 0.0015, 1, 10,
+            2, rix.ctypes.data, 4, 2, out_d.data_ptr(), None)
+    assert rc == 1 and b"not device memory" in lib.w2d_last_error()
+    rc = fn(v_d.data_ptr(), w_d.data_ptr(), nt, nx, nz, 5.0, 5.0, 5e-4, 10, 0.0015, 1, 10, 2,
+            rix.ctypes.data, 4, 2, out_d.data_ptr(), None)
+    assert rc == 0, lib.w2d_last_error()
