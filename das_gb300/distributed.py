@@ -7,8 +7,10 @@ reduction of the (nz, nx) stacked image and illumination follows, then the
 post-stack steps (mute, normalisation, Laplacian: rtm_engine.py:145-171).
 
 Two reductions:
-* ``"ordered"`` gathers every shot's image and illumination on rank 0 and stacks
-  them in shot order, reproducing the serial stack bit for bit;
+* ``"ordered"`` sends every shot's image and illumination to rank 0 alone (point
+  to point, as tensors, in shot order), which stacks them in the serial loop's
+  order -- bit for bit the serial stack -- and broadcasts the one stacked pair to
+  every rank;
 * ``"sum"`` sums each rank's partial stack with one all-reduce (less traffic;
   float32 addition order differs from the serial loop, so equal within
   rounding).
@@ -64,17 +66,12 @@ def migrate_multiple_shots_distributed(engine, flood_models, source_waveforms: S
     stacked = np.zeros(shape, np.float32)
     illum = np.zeros(shape, np.float32)
     if reduce == "ordered":
-        gathered = [results]
-        if world > 1:
-            gathered = [None] * world
-            dist.all_gather_object(gathered, {k: (np.asarray(a), np.asarray(b))
-                                              for k, (a, b) in results.items()})
-        allres = {}
-        for part in gathered:
-            allres.update(part)
-        for k in range(n):  # the serial loop's addition order
-            stacked += allres[k][0]
-            illum += allres[k][1]
+        if world == 1:
+            for k in range(n):  # the serial loop's addition order
+                stacked += results[k][0]
+                illum += results[k][1]
+        else:
+            stacked, illum = _ordered_stack(dist, rank, world, n, results, shape)
     elif reduce == "sum":
         for k in mine:
             stacked += results[k][0]
@@ -89,3 +86,39 @@ def migrate_multiple_shots_distributed(engine, flood_models, source_waveforms: S
     else:
         raise ValueError("reduce must be 'ordered' or 'sum'")
     return post_stack_fn(stacked, illum)
+
+
+def _ordered_stack(dist, rank: int, world: int, n: int, results: dict, shape):
+    """Stack every shot's (image, illumination) in shot order on rank 0, then broadcast.
+
+    Shot k lives on rank k % world.  Each rank sends its shots to rank 0 in
+    increasing k; rank 0 receives them in that order too, so it never holds more
+    than one remote pair at a time, and adds them in the serial loop's order.  One
+    broadcast of the stacked pair follows.  Traffic: every remote shot once to rank
+    0, then one (2, nz, nx) tensor to each rank.
+    """
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    stacked = np.zeros(shape, np.float32)
+    illum = np.zeros(shape, np.float32)
+    buf = torch.empty((2,) + tuple(shape), dtype=torch.float32, device=dev)
+    for k in range(n):
+        owner = k % world
+        if rank == 0:
+            if owner == 0:
+                a, b = results[k]
+            else:
+                dist.recv(buf, src=owner)
+                pair = buf.cpu().numpy()
+                a, b = pair[0], pair[1]
+            stacked += np.asarray(a, np.float32)
+            illum += np.asarray(b, np.float32)
+        elif owner == rank:
+            a, b = results[k]
+            buf.copy_(torch.from_numpy(np.stack([np.asarray(a, np.float32),
+                                                 np.asarray(b, np.float32)])))
+            dist.send(buf, dst=0)
+    out = torch.from_numpy(np.stack([stacked, illum])).to(dev)
+    dist.broadcast(out, src=0)
+    out = out.cpu().numpy()
+    return out[0].copy(), out[1].copy()

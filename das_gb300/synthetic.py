@@ -110,6 +110,21 @@ def plain_large(seed: int = 0, nt: int = 8000, n_shots: int = 200) -> Survey:
                   SURFACE_IZ, w, {"seed": seed, "faults": faults})
 
 
+def plain_large_window(n_steps: int = 240, first_sample: int = 560, seed: int = 0) -> Survey:
+    """The 1000 x 4000 survey cut to ``n_steps`` time steps for checks that a CPU
+    restatement must finish in seconds: the same grid, models, sponge, receivers and
+    sources, with the 6 Hz Ricker taken from ``first_sample`` on (its main lobe, which
+    peaks at sample 667, falls inside the window instead of after it)."""
+    sv = plain_large(seed=seed, nt=8000)
+    w = np.ascontiguousarray(sv.wavelet[first_sample:first_sample + n_steps])
+    sv.name = (f"large plain 2D acoustic RTM 1000x4000 cut to {len(w)} steps "
+               f"(Ricker from sample {first_sample}), 4000 receivers")
+    sv.wavelet = w
+    sv.nt = len(w)
+    sv.meta = dict(sv.meta, first_sample=first_sample)
+    return sv
+
+
 @dataclass
 class Gather:
     nz: int

@@ -1,0 +1,139 @@
+"""Parity at the benchmark configurations themselves, not stand-ins.
+
+* The 150 x 400 survey (dx 10 m; vp 1500 -> 3000 m/s with depth, a 200 m +400 m/s
+  layer at 700 m cut by a 60-degree fault with 100 m throw; migration model
+  Gaussian-smoothed with sigma 5 cells; 20 sources every 20 columns from column 10
+  on row 2; 400 receivers on row 2; 3 Hz Ricker, dt 1 ms, nt 2000; 40-cell sponge).
+  The observed gathers are forward-modelled in the true model, then all 20 shots
+  are migrated through ``TSWRTMEngine.migrate_multiple_shots`` -- the reference's
+  own driver shape (run_synthetic_benchmarks.py:50-70 -> rtm_engine.py:106-171) --
+  in both the batched form (the default for a grid this small) and the serial
+  per-shot loop.  Both are compared with the oracle's serial loop: gathers, raw and
+  normalised images bit for bit, the Laplacian within the image tolerance (scipy's
+  convolution sums in its own order).  Each image's error against a float64 run of
+  the same stencil is stated.
+* The 1000 x 4000 grid (dx 2.5 m, 4000 receivers, 40-cell sponge, the faulted
+  layered model scaled to depth) cut to 240 time steps: two shots (one inside the
+  sponge frame, one mid-line) through ``migrate_multiple_shots`` with the forward
+  wavefield kept whole (``all``) and recovered from checkpoints (``checkpoint``),
+  against the oracle bit for bit.
+
+Tolerances: traces 1e-5 relative L2, images 1e-4; where the float32 results are
+bit-identical the maximum absolute difference is asserted to be zero.
+"""
+import time
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+
+pytestmark = pytest.mark.gpu
+
+TRACE_TOL = 1e-5
+IMG_TOL = 1e-4
+
+
+def _exact(got, want, tol, what):
+    err = o.rel_l2(got, want)
+    assert err <= tol, f"{what}: rel L2 {err:.3e} > {tol}"
+    np.testing.assert_array_equal(got, want, err_msg=what)
+    return err
+
+
+def _grid(sv):
+    return o.Grid(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
+
+
+def _solver(sv):
+    from das_gb300.wave_solver import WaveSolver2D
+    return WaveSolver2D(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
+
+
+def _observed(sv, solver, grid, shots):
+    """Forward-modelled gathers in the true model: GPU, checked against the oracle."""
+    gathers = []
+    for six in shots:
+        rec, _ = solver.forward_propagate_acoustic(sv.vel_true, sv.wavelet, int(six), sv.src_iz,
+                                                   sv.rec_ix, sv.rec_iz)
+        want, _ = o.forward_propagate_acoustic(grid, sv.vel_true, sv.wavelet, int(six),
+                                               sv.src_iz, sv.rec_ix, sv.rec_iz)
+        _exact(rec, want, TRACE_TOL, f"gather of the source at column {six}")
+        gathers.append(rec)
+    return gathers
+
+
+def _images(res):
+    return {"raw": res.raw_image, "normalized": res.normalized_image,
+            "laplacian": res.laplacian_image}
+
+
+def test_config_150x400_twenty_shots(capsys):
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.synthetic import plain_small
+    from das_gb300.velocity_flood import FloodModels
+    t0 = time.perf_counter()
+    sv = plain_small()
+    assert (sv.nz, sv.nx, sv.nt, len(sv.src_ix), len(sv.rec_ix)) == (150, 400, 2000, 20, 400)
+    assert list(sv.src_ix) == list(range(10, 400, 20))
+    grid = _grid(sv)
+    s = _solver(sv)
+    gathers = _observed(sv, s, grid, sv.src_ix)
+    fm = FloodModels(sv.vel_true, sv.vel_mig, sv.vel_mig, 0, 0)
+    args = ([sv.wavelet] * 20, [int(v) for v in sv.src_ix], [sv.src_iz] * 20, gathers, sv.rec_ix,
+            sv.rec_iz, 2)
+    want = _images(o.migrate_multiple_shots(grid, sv.vel_mig, sv.vel_mig, *args))
+    want64 = _images(o.migrate_multiple_shots(grid, sv.vel_mig, sv.vel_mig, *args,
+                                              precision="f64"))
+    report = []
+    for batch in ("auto", "off"):
+        eng = TSWRTMEngine(s, batch=batch)
+        got = _images(eng.migrate_multiple_shots(fm, *args))
+        eng.close()
+        for k in ("raw", "normalized"):
+            _exact(got[k], want[k], IMG_TOL, f"{k} image (batch={batch})")
+        lap = o.rel_l2(got["laplacian"], want["laplacian"])
+        assert lap <= IMG_TOL, f"laplacian (batch={batch}): {lap:.3e}"
+        for k in got:
+            e64 = o.rel_l2(got[k], want64[k])
+            assert e64 <= IMG_TOL, f"{k} vs float64: {e64:.3e}"
+            report.append(f"{k}[batch={batch}] vs f64 {e64:.2e}")
+    s.close()
+    with capsys.disabled():
+        print(f"\n150x400 survey, 20 shots: {'; '.join(report)}; "
+              f"{time.perf_counter() - t0:.0f} s")
+
+
+@pytest.mark.parametrize("storage", ["all", "checkpoint"])
+def test_config_1000x4000_grid_cut(storage, capsys):
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.synthetic import plain_large_window
+    from das_gb300.velocity_flood import FloodModels
+    t0 = time.perf_counter()
+    sv = plain_large_window(240)
+    assert (sv.nz, sv.nx, sv.dx, len(sv.rec_ix), sv.n_sponge) == (1000, 4000, 2.5, 4000, 40)
+    grid = _grid(sv)
+    s = _solver(sv)
+    shots = [int(sv.src_ix[0]), int(sv.src_ix[117])]  # column 10 (in the sponge), mid-line
+    gathers = _observed(sv, s, grid, shots)
+    fm = FloodModels(sv.vel_true, sv.vel_mig, sv.vel_mig, 0, 0)
+    args = ([sv.wavelet] * 2, shots, [sv.src_iz] * 2, gathers, sv.rec_ix, sv.rec_iz, 2)
+    eng = TSWRTMEngine(s, storage=storage)
+    got = _images(eng.migrate_multiple_shots(fm, *args))
+    assert s.last_stats()["storage"] == storage
+    want = _images(o.migrate_multiple_shots(grid, sv.vel_mig, sv.vel_mig, *args))
+    for k in ("raw", "normalized"):
+        _exact(got[k], want[k], IMG_TOL, f"{k} image ({storage})")
+    assert o.rel_l2(got["laplacian"], want["laplacian"]) <= IMG_TOL
+    assert np.abs(got["raw"]).max() > 0
+    # float64 error of one shot's image and illumination (the second shot, mid-line)
+    img, ill = eng.migrate_shot(fm, sv.wavelet, shots[1], sv.src_iz, gathers[1], sv.rec_ix,
+                                sv.rec_iz, 2)
+    img64, ill64 = o.migrate_shot(grid, sv.vel_mig, sv.vel_mig, sv.wavelet, shots[1], sv.src_iz,
+                                  gathers[1], sv.rec_ix, sv.rec_iz, 2, precision="f64")
+    e_img, e_ill = o.rel_l2(img, img64), o.rel_l2(ill, ill64)
+    assert e_img <= IMG_TOL and e_ill <= IMG_TOL, (e_img, e_ill)
+    s.close()
+    with capsys.disabled():
+        print(f"\n1000x4000 grid, 240 steps, {storage}: image vs f64 {e_img:.2e}, "
+              f"illumination vs f64 {e_ill:.2e}; {time.perf_counter() - t0:.0f} s")
