@@ -204,16 +204,20 @@ def cpu_sample(sv, gather, nt_sample, threads):
     os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import oracle as o
     kind = "reference" if o.reference_available() else "port"
+    prev = o.backend()
     o.set_backend("reference" if kind == "reference" else "native")
     o.set_num_threads(threads)
     g = o.Grid(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
     sponge = g.sponge()
     w = sv.wavelet[:nt_sample]
     data = np.ascontiguousarray(gather[:nt_sample])
-    t0 = time.perf_counter()
-    o.migrate_shot(g, sv.vel_mig, sv.vel_mig, w, int(sv.src_ix[0]), sv.src_iz, data, sv.rec_ix,
-                   sv.rec_iz, 2, sponge=sponge, native=True)
-    el = time.perf_counter() - t0
+    try:
+        t0 = time.perf_counter()
+        o.migrate_shot(g, sv.vel_mig, sv.vel_mig, w, int(sv.src_ix[0]), sv.src_iz, data,
+                       sv.rec_ix, sv.rec_iz, 2, sponge=sponge, native=True)
+        el = time.perf_counter() - t0
+    finally:
+        o.set_backend(prev)  # the parity checks use the bit-exact restatement
     pts = 2 * sv.nz * sv.nx * nt_sample
     return pts / el / 1e9, el, kind
 
@@ -277,6 +281,7 @@ def accuracy_statement(storage="auto"):
     from das_gb300.synthetic import plain_large_window
     from das_gb300.velocity_flood import FloodModels
     from das_gb300.wave_solver import WaveSolver2D
+    o.set_backend("port")  # the restatement without FMA contraction: the reference's rounding
     sv = plain_large_window(240)
     six = int(sv.src_ix[117])
     grid = o.Grid(sv.nx, sv.nz, sv.dx, sv.dz, sv.dt, sv.n_sponge, sv.sponge_alpha, True)
@@ -479,16 +484,20 @@ def cpu_job_rate(job, nt_sample):
     os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import oracle as o
     kind = "reference" if o.reference_available() else "port"
+    prev = o.backend()
     o.set_backend("reference" if kind == "reference" else "native")
     o.set_num_threads(threads)
     g = o.Grid(job.nx, job.nz, job.dx, job.dz, job.dt, job.n_sponge, job.sponge_alpha,
                job.free_surface_top)
     n = min(nt_sample, len(job.wavelet))
-    t0 = time.perf_counter()
-    o.migrate_shot(g, job.vel_fwd, job.vel_bwd, job.wavelet[:n], job.source_ix, job.source_iz,
-                   np.ascontiguousarray(job.data[:n]), job.receiver_ix, job.receiver_iz,
-                   job.snapshot_interval, sponge=g.sponge(), native=True)
-    el = time.perf_counter() - t0
+    try:
+        t0 = time.perf_counter()
+        o.migrate_shot(g, job.vel_fwd, job.vel_bwd, job.wavelet[:n], job.source_ix,
+                       job.source_iz, np.ascontiguousarray(job.data[:n]), job.receiver_ix,
+                       job.receiver_iz, job.snapshot_interval, sponge=g.sponge(), native=True)
+        el = time.perf_counter() - t0
+    finally:
+        o.set_backend(prev)
     return 2.0 * job.nx * job.nz * n / el / 1e9, el, threads, kind
 
 
@@ -684,16 +693,21 @@ def run_served(args, dist):
     eng.run([s for r in trace if r.kind == "acoustic" for s in r.shots][:1])  # graph capture
     ex = ElasticExecutor()
     out, st = RTMServer(eng, elastic_executor=ex).serve(trace, realtime=True)
+    st["elastic_worker_busy_s"] = ex.busy_s
+    st["acoustic_device_busy_s"] = st["device_busy_frac"] * st["makespan_s"]
+    ex.busy_s = 0.0
     eng.close()
     # plain per-shot loop over the same trace (or its first --plain-jobs jobs), FIFO,
     # arrivals on the wall clock
     m = len(trace) if args.plain_jobs <= 0 else min(args.plain_jobs, len(trace))
     t0 = time.perf_counter()
     lat, shots_done = [], 0
+    kind_s = {"acoustic": 0.0, "elastic": 0.0}
     for r in trace[:m]:
         wait = r.arrival - (time.perf_counter() - t0)
         if wait > 0:
             time.sleep(wait)
+        tj = time.perf_counter()
         j0 = r.shots[0]
         if r.kind == "elastic":
             es = ElasticSolver2D(j0.nx, j0.nz, j0.dx, j0.dz, j0.dt, j0.n_sponge, j0.sponge_alpha,
@@ -711,11 +725,13 @@ def run_served(args, dist):
                                2)
                 shots_done += 1
             s.close()
+        kind_s[r.kind] += time.perf_counter() - tj
         lat.append(time.perf_counter() - t0 - r.arrival)
     ex.close()
     plain_span = time.perf_counter() - t0
     plain = {"jobs": m, "shots": shots_done, "shots_per_s": shots_done / plain_span,
-             "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99)}
+             "p50_latency_s": percentile(lat, 50), "p99_latency_s": percentile(lat, 99),
+             "busy_s_by_kind": kind_s}
     served_first = [x.latency for x in out[:m]]
     plain["makespan_s"] = plain_span
     out_line = {"metric": "served RTM shots/s", "value": st["shots_per_s"], "unit": "shots/s",

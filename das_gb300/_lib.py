@@ -74,6 +74,7 @@ _SIGS = {
     "w2d_fwi_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int,
                                 c_int, c_void_p]),
     "w2d_fwi_gradient": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "w2d_fwi_set_segment": (c_int, [c_void_p, c_int]),
     "w2d_engine_synchronize": (c_int, [c_void_p]),
     "w2d_elastic_create": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_float, c_float,
                                    ctypes.c_double, c_int, c_float, c_int]),

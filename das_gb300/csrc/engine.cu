@@ -112,6 +112,7 @@ struct w2d_engine {
     TileShape tile{4, 4};
     int l2_hints = 0;
     int persistent = 0, pdl = 1;  // step launch mode (measured fastest: one CTA per tile + PDL)
+    int fwi_seg = 0;  // differentiable path: steps per checkpoint segment (0: sqrt(3 nt))
     bool chain = false;  // the last operation on the stream is a step kernel launched by step()
     DevBuf<unsigned> tile_counter;
     unsigned counter_base = 0;
@@ -1314,6 +1315,7 @@ bool written_cell(const w2d_engine* e, int iz, int ix)
 
 struct w2d_fwi_state {
     int nt = 0, n_rec = 0, seg = 0, n_seg = 0;
+    bool stored = false;  // one segment of every forward state, written by the forward pass
     DevBuf<float> vel_p, grad_c, zero, segbuf;
     std::vector<CUtensorMap> seg_maps;
     CUtensorMap map_c_halo, map_zero;
@@ -1344,7 +1346,7 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
     if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
     f->nt = nt;
     f->n_rec = n_rec;
-    f->seg = std::max(1, (int)std::sqrt(3.0 * nt));
+    f->seg = e->fwi_seg > 0 ? std::min(e->fwi_seg, nt) : std::max(1, (int)std::sqrt(3.0 * nt));
     f->n_seg = (nt + f->seg - 1) / f->seg;
     if ((rc = f->vel_p.ensure(e->plane)) || (rc = f->grad_c.ensure(e->plane)) ||
         (rc = f->zero.ensure(e->plane)) || (rc = f->segbuf.ensure((size_t)f->seg * e->plane)) ||
@@ -1367,12 +1369,28 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
     o.nt = nt;
     o.n_rec = n_rec;
     o.rec_out = e->rec_out.p;
-    o.ckpt = e->ckpt.p;
-    o.ckpt_every = f->seg;
+    f->stored = f->seg >= nt;
+    if (f->stored) {
+        // every forward state kept as it is computed: the gradient recomputes nothing
+        o.snaps = f->segbuf.p;
+        o.interval = 1;
+        o.slot0 = 0;
+    } else {
+        o.ckpt = e->ckpt.p;
+        o.ckpt_every = f->seg;
+    }
     if ((rc = run_forward_steps(e, 0, o, 0, nt, 0.0, dt2inj))) return rc;
     W2D_CUDA_TRY(cudaMemcpyAsync(traces_dev, e->rec_out.p, (size_t)nt * n_rec * 4,
                                  cudaMemcpyDeviceToDevice, e->stream));
     return check_err(e);
+}
+
+int w2d_fwi_set_segment(w2d_engine* e, int steps)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CHECK_ARG(steps >= 0, "segment length must be >= 0");
+    e->fwi_seg = steps;
+    return W2D_OK;
 }
 
 int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
@@ -1423,19 +1441,22 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
     const float dt2inj = (float)(e->dt_d * e->dt_d);
     for (int sgi = f->n_seg - 1; sgi >= 0; --sgi) {
         const int a = sgi * seg, b = std::min(nt, a + seg);
-        const float* c = e->ckpt.p + (size_t)sgi * 3 * e->plane;
-        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave(a % 3), c, plane_b, cudaMemcpyDeviceToDevice, e->stream));
-        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 1) % 3), c + e->plane, plane_b,
-                                     cudaMemcpyDeviceToDevice, e->stream));
-        W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 2) % 3), c + 2 * e->plane, plane_b,
-                                     cudaMemcpyDeviceToDevice, e->stream));
-        FwdOpts r;
-        r.nt = nt;
-        r.interval = 1;
-        r.snaps = f->segbuf.p;
-        r.slot0 = a;
-        if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
-        e->last_recompute += b - a;
+        if (!f->stored) {
+            const float* c = e->ckpt.p + (size_t)sgi * 3 * e->plane;
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave(a % 3), c, plane_b, cudaMemcpyDeviceToDevice,
+                                         e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 1) % 3), c + e->plane, plane_b,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            W2D_CUDA_TRY(cudaMemcpyAsync(e->wave((a + 2) % 3), c + 2 * e->plane, plane_b,
+                                         cudaMemcpyDeviceToDevice, e->stream));
+            FwdOpts r;
+            r.nt = nt;
+            r.interval = 1;
+            r.snaps = f->segbuf.p;
+            r.slot0 = a;
+            if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
+            e->last_recompute += b - a;
+        }
         for (int n = b - 1; n >= a; --n)
             if ((rc = adj(n, f->seg_maps[n - a]))) return rc;
     }

@@ -165,6 +165,7 @@ class ElasticExecutor:
         self._pending = 0
         self._jobs = {}  # job_id -> [request, results, shots left]
         self._solvers = {}
+        self.busy_s = 0.0  # summed wall time of the workers' batches
         self.budget = int(budget_gb * (1 << 30))  # device bytes per worker for one batch
         # the creating thread's device: the CUDA device is per host thread and a new
         # thread starts on device 0, so each worker selects this one before any CUDA call
@@ -253,8 +254,10 @@ class ElasticExecutor:
                 s0 = shots[0]
                 solver = ElasticSolver2D(s0.nx, s0.nz, s0.dx, s0.dz, s0.dt, s0.n_sponge,
                                          s0.sponge_alpha, s0.free_surface_top)
+            tb = time.perf_counter()
             res = self.migrate_shots(solver, shots)
             with self._lock:
+                self.busy_s += time.perf_counter() - tb
                 entry = self._jobs[jid]
                 for k, r in zip(ks, res):
                     entry[1][k] = r

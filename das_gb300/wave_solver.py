@@ -121,6 +121,12 @@ class WaveSolver2D:
             v = (1 if on else 0) if isinstance(on, bool) else int(on)
             _lib.check(self._lib.w2d_engine_set_two_step(self._engine, v))
 
+    def set_checkpoint_segment(self, steps: int = 0) -> None:
+        """Steps per checkpoint segment of the differentiable path (das_gb300.autograd):
+        0 picks sqrt(3 nt); nt or more stores every forward state (no recomputation).
+        The gradient is the same bit for bit either way."""
+        _lib.check(self._lib.w2d_fwi_set_segment(self._eng(), int(steps)))
+
     def close(self):
         if getattr(self, "_engine", None) is not None:
             self._lib.w2d_engine_destroy(self._engine)

@@ -189,6 +189,11 @@ int w2d_fwi_forward(w2d_engine* e, const float* vel_dev, const float* wavelet, i
  * (DEVICE, nz x nx, overwritten).  Hand-written adjoint kernel; the forward
  * wavefield is recomputed segment by segment from the checkpoints. */
 int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev);
+/* Steps per checkpoint segment of the next w2d_fwi_forward: 0 (the default) picks
+ * sqrt(3 nt), the segment length that balances checkpoint and segment storage;
+ * nt or more keeps every forward state of the run (no recomputation, nt planes
+ * of device memory).  The gradient is the same bit for bit either way. */
+int w2d_fwi_set_segment(w2d_engine* e, int steps);
 int w2d_engine_synchronize(w2d_engine* e);
 
 /* ---- Elastic modelling and gradient (no reference counterpart: the reference only

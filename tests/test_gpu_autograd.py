@@ -63,7 +63,7 @@ def test_gradient_matches_finite_differences():
     fd, an = np.array(fd), np.array(an)
     err = np.linalg.norm(an - fd) / np.linalg.norm(fd)
     print(f"gradient vs central differences on 16 cells: rel-L2 {err:.2e}")
-    assert err < 2e-2, (an, fd)
+    assert err < 1e-3, (an, fd)
 
 
 def test_gradient_relates_to_rtm_image():
@@ -80,13 +80,16 @@ def test_gradient_relates_to_rtm_image():
     m = (slice(8, 40), slice(12, 88))
     c = np.corrcoef(g[m].ravel(), img[m].ravel())[0, 1]
     print(f"correlation(gradient, RTM image of the residual) = {c:.3f}")
-    assert c < -0.6  # d2/dt2 ~ -omega^2: anti-correlated with the zero-lag image
+    assert c < -0.8  # d2/dt2 ~ -omega^2: anti-correlated with the zero-lag image
 
 
 def test_gradient_of_8000_steps_on_the_large_grid():
-    """An 8000-step shot on the 1000 x 4000 grid: the forward states come back from
-    checkpoints (about sqrt(3 nt) segments of recomputation), so the gradient fits in
-    HBM; it is finite, non-zero, and its run time is reported."""
+    """An 8000-step shot on the 1000 x 4000 grid.  By default the forward states come
+    back from checkpoints (about sqrt(3 nt) steps per segment, one segment of states
+    stored at a time), so the gradient fits in a few GB of HBM.  The same gradient
+    with every forward state stored by the forward pass itself (8000 planes, 128 GB:
+    nothing recomputed) must be equal bit for bit, because the recomputation replays
+    the same kernels on the same inputs."""
     import time
     from das_gb300.autograd import misfit_and_gradient
     from das_gb300.wave_solver import WaveSolver2D, ricker_wavelet
@@ -99,10 +102,20 @@ def test_gradient_of_8000_steps_on_the_large_grid():
     t0 = time.perf_counter()
     J, g = misfit_and_gradient(s, v, w, nx // 2, 2, rix, 2, d_obs)
     el = time.perf_counter() - t0
-    print(f"8000-step gradient on 1000 x 4000: {el:.2f} s, J = {J:.3e}")
+    st = s.last_stats()
     assert np.isfinite(J) and J > 0
     assert np.isfinite(g).all() and np.abs(g).max() > 0
+    assert st["recomputed_steps"] == nt  # each segment recomputed once from its checkpoint
+    s.set_checkpoint_segment(nt)
+    t0 = time.perf_counter()
+    J_full, g_full = misfit_and_gradient(s, v, w, nx // 2, 2, rix, 2, d_obs)
+    el_full = time.perf_counter() - t0
+    assert s.last_stats()["recomputed_steps"] == 0
     s.close()
+    print(f"8000-step gradient on 1000 x 4000: checkpointed {el:.2f} s "
+          f"({st['recomputed_steps']} steps recomputed), all states stored {el_full:.2f} s")
+    assert J_full == J
+    np.testing.assert_array_equal(g_full, g)
 
 
 def test_device_arguments_refuse_host_memory():

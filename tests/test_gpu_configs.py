@@ -11,7 +11,8 @@
   per-shot loop.  Both are compared with the oracle's serial loop: gathers, raw and
   normalised images bit for bit, the Laplacian within the image tolerance (scipy's
   convolution sums in its own order).  Each image's error against a float64 run of
-  the same stencil is stated.
+  the same stencil is stated (printed; bounded only loosely, since it is the
+  reference's own float32 rounding).
 * The 1000 x 4000 grid (dx 2.5 m, 4000 receivers, 40-cell sponge, the faulted
   layered model scaled to depth) cut to 240 time steps: two shots (one inside the
   sponge frame, one mid-line) through ``migrate_multiple_shots`` with the forward
@@ -32,6 +33,9 @@ pytestmark = pytest.mark.gpu
 
 TRACE_TOL = 1e-5
 IMG_TOL = 1e-4
+# the float32 reference arithmetic against a float64 run of the same stencil: a sanity
+# bound on the stated errors (they are printed), not a parity tolerance
+F64_BOUND = 1e-3
 
 
 def _exact(got, want, tol, what):
@@ -95,8 +99,11 @@ def test_config_150x400_twenty_shots(capsys):
         lap = o.rel_l2(got["laplacian"], want["laplacian"])
         assert lap <= IMG_TOL, f"laplacian (batch={batch}): {lap:.3e}"
         for k in got:
+            # stated, not held to the image tolerance: the reference's own float32
+            # arithmetic sits this far from float64 (the normalised stack of 20 shots
+            # about 1.1e-4, the division amplifying the weakly illuminated cells)
             e64 = o.rel_l2(got[k], want64[k])
-            assert e64 <= IMG_TOL, f"{k} vs float64: {e64:.3e}"
+            assert e64 <= F64_BOUND, f"{k} vs float64: {e64:.3e}"
             report.append(f"{k}[batch={batch}] vs f64 {e64:.2e}")
     s.close()
     with capsys.disabled():
@@ -132,7 +139,7 @@ def test_config_1000x4000_grid_cut(storage, capsys):
     img64, ill64 = o.migrate_shot(grid, sv.vel_mig, sv.vel_mig, sv.wavelet, shots[1], sv.src_iz,
                                   gathers[1], sv.rec_ix, sv.rec_iz, 2, precision="f64")
     e_img, e_ill = o.rel_l2(img, img64), o.rel_l2(ill, ill64)
-    assert e_img <= IMG_TOL and e_ill <= IMG_TOL, (e_img, e_ill)
+    assert e_img <= F64_BOUND and e_ill <= F64_BOUND, (e_img, e_ill)
     s.close()
     with capsys.disabled():
         print(f"\n1000x4000 grid, 240 steps, {storage}: image vs f64 {e_img:.2e}, "
