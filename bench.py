@@ -376,6 +376,7 @@ def run_ours(args, dist):
     ms = ctypes.c_float()
     _lib.check(lib.w2d_engine_timer_stop(eng, ctypes.byref(ms)))
     wall = time.perf_counter() - t_wall
+    free_b, total_b = _lib.device_memory()  # the engine still holds its buffers here
     dist.barrier()
     clk = clocks.stop()
     dev_s = dist.max(ms.value / 1e3)
@@ -438,6 +439,8 @@ def run_ours(args, dist):
                           "launch": args.launch, "pdl": bool(args.pdl),
                           "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
                "shots_per_s": K * dist.world / dev_s,
+               "recomputed_steps_per_shot": recompute / max(K, 1),
+               "device_memory_in_use_gb": (total_b - free_b) / 1e9,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
                             "peak_source": f"{peak_kind} hbm_gbs",
@@ -661,6 +664,14 @@ def run_elastic(args, dist):
             fwd_ms.append(f_ms)
             grad_ms.append(solver.last_ms)
     pts = 2.0 * nz * nx * nt
+    # roofline of the gradient phase (the device time of J.backward): per time step and
+    # grid point the recomputation moves 56 B (the forward step: five fields read and
+    # written, lambda, mu and the two buoyancies read) + 20 B (the five fields stored
+    # into the segment), and the two tiled adjoint passes 28 + 14 planes = 168 B
+    peak, peak_kind = measured_peaks()
+    grad_bytes = nz * nx * nt * (56 + 20 + 168)
+    achieved = grad_bytes / (statistics.mean(grad_ms) / 1e3) / 1e9
+    fwd_achieved = nz * nx * nt * 56 / (statistics.mean(fwd_ms) / 1e3) / 1e9
     out = {"metric": "elastic RTM gradient Gpts/s", "value": pts * K / sum(times) / 1e9,
            "unit": "Gpts/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
            "data": "synthetic", "steps": K, "warmup": W,
@@ -669,7 +680,15 @@ def run_elastic(args, dist):
                       "adjoint": args.el_adjoint, "tiles": args.el_tiles},
            "s_per_shot": sum(times) / K, "device_ms_forward": statistics.mean(fwd_ms),
            "device_ms_gradient": statistics.mean(grad_ms),
-           "counted_points_per_shot": pts}
+           "counted_points_per_shot": pts,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "peak_source": f"{peak_kind} hbm_gbs",
+                        "kernel": "gradient phase: el_adj_a + el_adj_b (tiled adjoint passes) "
+                                  "and the segment recomputation's step kernels",
+                        "algorithmic_bytes_per_step_point": 56 + 20 + 168,
+                        "forward_phase_achieved_gbs": fwd_achieved,
+                        "forward_phase_frac": fwd_achieved / peak}}
     print(json.dumps(out), flush=True)
 
 

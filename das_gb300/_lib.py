@@ -75,6 +75,8 @@ _SIGS = {
                                 c_int, c_void_p]),
     "w2d_fwi_gradient": (c_int, [c_void_p, c_void_p, c_void_p]),
     "w2d_fwi_set_segment": (c_int, [c_void_p, c_int]),
+    "w2d_flood_models": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.c_double,
+                                 ctypes.c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "w2d_engine_synchronize": (c_int, [c_void_p]),
     "w2d_elastic_create": (c_int, [ctypes.POINTER(c_void_p), c_int, c_int, c_float, c_float,
                                    ctypes.c_double, c_int, c_float, c_int]),

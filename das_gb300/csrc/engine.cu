@@ -187,6 +187,28 @@ int upload_field(w2d_engine* e, float* dst_pitched, const float* host)
     return W2D_OK;
 }
 
+// A contiguous (nz, nx) field that may be host memory or device memory of the engine's
+// device (a device-resident model): into a pitched plane.
+int upload_field_any(w2d_engine* e, float* dst_pitched, const float* src)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, src) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA pointer: pageable host memory
+        return upload_field(e, dst_pitched, src);
+    }
+    if (a.type == cudaMemoryTypeDevice && a.device != e->device) {
+        set_error("velocity model is on device " + std::to_string(a.device) + ", the engine on " +
+                  std::to_string(e->device));
+        return W2D_EINVAL;
+    }
+    const cudaMemcpyKind kind = (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+                                    ? cudaMemcpyDeviceToDevice
+                                    : cudaMemcpyHostToDevice;
+    W2D_CUDA_TRY(cudaMemcpy2DAsync(dst_pitched, (size_t)e->ldx * 4, src, (size_t)e->nx * 4,
+                                   (size_t)e->nx * 4, e->nz, kind, e->stream));
+    return W2D_OK;
+}
+
 int download_field(w2d_engine* e, float* host, const float* src_pitched)
 {
     W2D_CUDA_TRY(cudaMemcpy2DAsync(host, (size_t)e->nx * 4, src_pitched, (size_t)e->ldx * 4,
@@ -729,7 +751,7 @@ int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel)
     W2D_CHECK_ARG(slot == 0 || slot == 1, "velocity slot must be 0 or 1");
     int rc;
     W2D_CUDA_TRY(cudaMemsetAsync(e->staging.p, 0, e->plane * 4, e->stream));
-    if ((rc = upload_field(e, e->staging.p, vel))) return rc;
+    if ((rc = upload_field_any(e, e->staging.p, vel))) return rc;
     v2dt2_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->v2dt2.p + (size_t)slot * e->plane,
                                                             e->staging.p, e->plane, e->dt2);
     W2D_CUDA_TRY(cudaGetLastError());

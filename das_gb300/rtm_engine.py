@@ -6,6 +6,8 @@
   sediment-flood model with snapshots and illumination, then back-propagation in the
   rock-flood model with zero-lag imaging, in ONE call into the library; the forward
   wavefield never leaves the device (kept whole, or checkpointed and recomputed).
+  The flood models may be host arrays or CUDA tensors already on the device (e.g.
+  from ``generate_velocity_flood_models_on_device``).
 * ``TSWRTMEngine.migrate_multiple_shots``  rtm_engine.py:106-171: the shot images are
   stacked on the device; sponge mute, illumination normalisation and the Laplacian
   run on the stacked image as the reference does.  On grids too small for one shot
@@ -154,13 +156,14 @@ class TSWRTMEngine:
         s = self.solver
         n_sp = s.n_sponge if s.sponge is not None else -1
         key = new_model_key()  # every shot migrates in the same flood models
+        v_sed, v_rock = _host(flood_models.sediment_flood), _host(flood_models.rock_flood)
         jobs = []
         for k in range(len(source_coords_ix)):
             w, data, rix, riz, six, siz = self._check(receiver_gathers[k], receiver_ix,
                                                       receiver_iz, source_waveforms[k],
                                                       source_coords_ix[k], source_coords_iz[k])
-            jobs.append(ShotJob(s.nx, s.nz, s.dx, s.dz, s.dt, flood_models.sediment_flood,
-                                flood_models.rock_flood, w, data, rix, six, siz, riz,
+            jobs.append(ShotJob(s.nx, s.nz, s.dx, s.dz, s.dt, v_sed, v_rock, w, data, rix, six,
+                                siz, riz,
                                 int(snapshot_interval), n_sp, s.sponge_alpha,
                                 bool(s.free_surface_top), model_key=key))
         per = max(BatchEngine.shot_bytes(j) for j in jobs)
@@ -188,6 +191,13 @@ class TSWRTMEngine:
             _lib.check(s._lib.w2d_migrate_shot(
                 eng, w.ctypes.data, len(w), six, siz, data.ctypes.data, rix.ctypes.data,
                 data.shape[1], riz, int(snapshot_interval), _STORAGE[self.storage], None, None))
+
+
+def _host(a):
+    """A model as a host array (a device-resident CUDA tensor is copied back)."""
+    if type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False):
+        return a.detach().float().contiguous().cpu().numpy()
+    return a
 
 
 def post_stack(solver: WaveSolver2D, stacked: np.ndarray, illum: np.ndarray,

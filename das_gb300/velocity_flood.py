@@ -53,3 +53,42 @@ def generate_velocity_flood_models(base_model: np.ndarray, fault_x_idx: int,
 
 def _wrap(cols: np.ndarray, nx: int) -> np.ndarray:
     return np.where(cols < 0, cols + nx, cols)
+
+
+def generate_velocity_flood_models_on_device(base_model, fault_x_idx: int,
+                                             sediment_is_left: bool = True,
+                                             flood_offset_cells: int = 15,
+                                             perturb_sediment: float = 0.0,
+                                             perturb_rock: float = 0.0) -> FloodModels:
+    """The flood models of a float32 CUDA tensor ``base_model`` (nz, nx), built on its
+    device: the same values as ``generate_velocity_flood_models`` on the same float32
+    base model.  The FloodModels fields are CUDA tensors (``true_model`` a copy of the
+    base); a flood line outside the model raises IndexError as the reference does."""
+    import ctypes
+    import torch
+    from . import _lib
+    if not (isinstance(base_model, torch.Tensor) and base_model.is_cuda):
+        raise TypeError("base_model must be a CUDA tensor")
+    if base_model.dtype != torch.float32 or base_model.dim() != 2:
+        raise TypeError("base_model must be a 2-D float32 tensor")
+    base = base_model.detach().contiguous()
+    nz, nx = base.shape
+    sed = torch.empty_like(base)
+    rock = torch.empty_like(base)
+    lines = (ctypes.c_int * 2)()
+    lib = _lib.load()
+    with torch.cuda.device(base.device):
+        stream = torch.cuda.current_stream(base.device).cuda_stream
+        rc = lib.w2d_flood_models(base.data_ptr(), nz, nx, int(fault_x_idx),
+                                  1 if sediment_is_left else 0, int(flood_offset_cells),
+                                  float(perturb_sediment), float(perturb_rock), sed.data_ptr(),
+                                  rock.data_ptr(), lines, ctypes.c_void_p(stream))
+    if rc != 0:
+        msg = lib.w2d_last_error()
+        msg = msg.decode() if isinstance(msg, bytes) else str(msg)
+        if "flood line" in msg:
+            raise IndexError(msg)
+        _lib.check(rc)
+    return FloodModels(true_model=base.clone(), sediment_flood=sed, rock_flood=rock,
+                       flood_line_sed=int(lines[0]), flood_line_rock=int(lines[1]))
+

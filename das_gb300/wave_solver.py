@@ -40,6 +40,11 @@ def _f32(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float32)
 
 
+def _is_cuda_tensor(a) -> bool:
+    mod = type(a).__module__
+    return mod.startswith("torch") and getattr(a, "is_cuda", False)
+
+
 class WaveSolver2D:
     """2D wavefield propagator on one GB300 (sm_103a) GPU."""
 
@@ -140,6 +145,19 @@ class WaveSolver2D:
             pass
 
     def _set_velocity(self, slot: int, velocity_model) -> None:
+        if _is_cuda_tensor(velocity_model):
+            # a device-resident model (e.g. from generate_velocity_flood_models_on_device):
+            # copied device to device, after the work that produced it on its stream
+            import torch
+            t = velocity_model.detach()
+            if t.dtype != torch.float32:
+                raise TypeError("a device velocity model must be float32")
+            t = t.contiguous()
+            if tuple(t.shape) != (self.nz, self.nx):
+                raise ValueError(f"velocity model shape {tuple(t.shape)} != {(self.nz, self.nx)}")
+            torch.cuda.current_stream(t.device).synchronize()
+            _lib.check(self._lib.w2d_engine_set_velocity(self._eng(), slot, t.data_ptr()))
+            return
         vel = _f32(velocity_model)
         if vel.shape != (self.nz, self.nx):
             raise ValueError(f"velocity model shape {vel.shape} != {(self.nz, self.nx)}")

@@ -92,7 +92,10 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
                       const float* sponge, int free_surface_top);
 void w2d_engine_destroy(w2d_engine* e);
 
-/* Velocity model for slot 0 (forward / sediment flood) or 1 (backward / rock flood). */
+/* Velocity model for slot 0 (forward / sediment flood) or 1 (backward / rock flood):
+ * contiguous nz x nx float32 in host memory, or in device memory of the engine's
+ * device (a device-resident model, copied device to device; memory of another GPU
+ * returns W2D_EINVAL).  Synchronous. */
 int w2d_engine_set_velocity(w2d_engine* e, int slot, const float* vel);
 
 /* Kernel tile shape (warps per CTA, rows per warp); 0,0 restores the default. */
@@ -172,6 +175,18 @@ int w2d_device_pci_bus_id(char* buf, int len);
 
 /* Free and total device memory of the current device, in bytes. */
 int w2d_device_memory(unsigned long long* free_bytes, unsigned long long* total_bytes);
+
+/* Velocity-flood models on the device (generate_velocity_flood_models,
+ * tsw_rtm/velocity_flood.py:24-94): from base_dev (DEVICE, contiguous nz x nx
+ * float32) write the sediment flood to sed_dev and the rock flood to rock_dev
+ * (DEVICE, nz x nx), with the reference's flood lines (returned in
+ * flood_lines[0..1] when not NULL) and its float32 perturbation arithmetic.
+ * Asynchronous on `stream` (a cudaStream_t, NULL: the default stream).  A flood
+ * line outside the model's columns (the reference raises IndexError) returns
+ * W2D_EINVAL. */
+int w2d_flood_models(const float* base_dev, int nz, int nx, int fault_x_idx, int sediment_is_left,
+                     int flood_offset_cells, double perturb_sediment, double perturb_rock,
+                     float* sed_dev, float* rock_dev, int* flood_lines, void* stream);
 
 /* Page-locked host memory for fast host<->device copies of shot inputs/outputs. */
 int w2d_host_alloc(void** out, unsigned long long bytes);

@@ -10,6 +10,7 @@ Restates, with numpy loops over the per-step C operators of
 * ``migrate_shot``                        tsw_rtm/rtm_engine.py:49-104
 * ``migrate_multiple_shots``              tsw_rtm/rtm_engine.py:106-171
 * ``apply_laplacian_filter``              tsw_rtm/rtm_engine.py:27-38
+* ``generate_velocity_flood_models``      tsw_rtm/velocity_flood.py:24-94
 
 Every function has a ``precision`` argument: ``"f32"`` follows the reference's
 float32 arithmetic step for step (injection products are float32 x float32
@@ -385,3 +386,41 @@ def gardner_parameters(vs, vp_over_vs=1.73, precision="f64"):
     lam = rho * vp * vp - dt_(2.0) * mu
     b = dt_(1.0) / rho
     return lam, mu, b, b
+
+
+# --------------------------------------------------------------------------- flood models
+
+def generate_velocity_flood_models(base_model, fault_x_idx, sediment_is_left=True,
+                                   flood_offset_cells=15, perturb_sediment=0.0,
+                                   perturb_rock=0.0):
+    """tsw_rtm/velocity_flood.py:24-94 step for step: slice copies, then the per-column
+    fill loops (Python indexing: a negative flood line counts from the end), then the
+    fractional perturbations.  Returns (sediment_flood, rock_flood, line_sed, line_rock)."""
+    base = np.asarray(base_model)
+    nz, nx = base.shape
+    sed = np.zeros_like(base)
+    rock = np.zeros_like(base)
+    if sediment_is_left:
+        ls = min(nx - 1, fault_x_idx - flood_offset_cells)
+        lr = max(0, fault_x_idx + flood_offset_cells)
+        sed[:, :ls] = base[:, :ls]
+        for ix in range(ls, nx):
+            sed[:, ix] = base[:, ls]
+        rock[:, lr:] = base[:, lr:]
+        for ix in range(0, lr):
+            rock[:, ix] = base[:, lr]
+    else:
+        ls = max(0, fault_x_idx + flood_offset_cells)
+        lr = min(nx - 1, fault_x_idx - flood_offset_cells)
+        sed[:, ls:] = base[:, ls:]
+        for ix in range(0, ls):
+            sed[:, ix] = base[:, ls]
+        rock[:, :lr] = base[:, :lr]
+        for ix in range(lr, nx):
+            rock[:, ix] = base[:, lr]
+    if perturb_sediment != 0.0:
+        sed = sed * (1.0 + perturb_sediment)
+    if perturb_rock != 0.0:
+        rock = rock * (1.0 + perturb_rock)
+    return sed.astype(np.float32), rock.astype(np.float32), ls, lr
+

@@ -137,3 +137,22 @@ def test_f64_close_to_f32(golden):
                                               np.arange(grid.nx), 2, True, 3, precision="f64")
     assert o.rel_l2(g["fwd_rec"], rec) < 1e-4
     assert o.rel_l2(g["fwd_snaps"], snaps) < 1e-4
+
+
+def test_flood_models_bitwise(golden):
+    """The oracle's flood construction (velocity_flood.py:24-94, its loops restated)
+    against the reference's own output, and the package's host port against the oracle
+    over both sides, negative flood lines and zero perturbations."""
+    g = golden("loops")
+    sed, rock, _, _ = o.generate_velocity_flood_models(g["vtrue"], 30, True, 6, 0.1, -0.05)
+    np.testing.assert_array_equal(sed, g["flood_sed"])
+    np.testing.assert_array_equal(rock, g["flood_rock"])
+    from das_gb300.velocity_flood import generate_velocity_flood_models
+    base = g["vtrue"]
+    for args in [(30, True, 6, 0.1, -0.05), (30, False, 6, 0.0, 0.2), (3, True, 10, -0.1, 0.0),
+                 (60, False, 2, 0.05, 0.05), (0, False, 0, 0.0, 0.0), (5, True, 9, 0.0, 0.0)]:
+        fl = generate_velocity_flood_models(base, *args)
+        sed, rock, ls, lr = o.generate_velocity_flood_models(base, *args)
+        np.testing.assert_array_equal(fl.sediment_flood, sed, err_msg=str(args))
+        np.testing.assert_array_equal(fl.rock_flood, rock, err_msg=str(args))
+        assert (fl.flood_line_sed, fl.flood_line_rock) == (ls, lr)
