@@ -485,75 +485,6 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-// Streaming form of the same tile-step: a grid sized to the resident capacity; CTA b
-// takes tiles b, b + G, b + 2G, ... (G CTAs: at each round the CTAs work on G
-// consecutive tiles, a band of tile rows whose halos neighbouring CTAs share in L2)
-// through a ring of STAGES shared-memory stages, each with its own mbarrier.  The
-// boxes of the next STAGES - 1 tiles are in flight while a tile is computed, and the
-// assignment is static, so no CTA waits on a counter before it issues a load.  Within
-// a step no tile reads what another writes (all read the previous step's planes), so
-// the order of tiles is free; the result is bit-identical to one CTA per tile.
-template <int WARPS, int RPW, int SPONGE, int STAGES>
-__global__ void __launch_bounds__(WARPS * 32)
-    acoustic_step_stream(const __grid_constant__ AcMaps maps, const AcGeom g, const AcStep s,
-                         int tiles_x, int ntiles)
-{
-    using T = AcTile<WARPS, RPW, SPONGE>;
-    extern __shared__ __align__(128) float smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * T::FLOATS);
-    const int tid = threadIdx.x;
-    const int G = gridDim.x;
-    if (tid == 0) {
-        prefetch_tensormap(&maps.curr);
-        prefetch_tensormap(&maps.prev);
-        prefetch_tensormap(&maps.vel);
-#pragma unroll
-        for (int k = 0; k < STAGES; ++k) mbar_init(bar + k, 1);
-        fence_mbar_init();
-    }
-    grid_dep_launch();
-    grid_dep_wait();
-    auto issue = [&](int t, int stage) {
-        const int x0 = (t % tiles_x) * AC_TX, z0 = (t / tiles_x) * T::TZ;
-        ac_issue_loads<WARPS, RPW, SPONGE>(smem + stage * T::FLOATS, &maps, x0, z0, bar + stage,
-                                           g.l2_hints);
-    };
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < STAGES; ++k) {
-            const int t = blockIdx.x + k * G;
-            if (t < ntiles) issue(t, k);
-        }
-    }
-    __syncthreads();
-    for (int i = 0;; ++i) {
-        const int t = blockIdx.x + i * G;
-        if (t >= ntiles) break;
-        const int st = i % STAGES;
-        const bool got = mbar_wait_bounded(bar + st, (unsigned)(i / STAGES) & 1u);
-        if (__syncthreads_or(!got)) {
-            if (tid == 0) {
-                atomicOr(s.err, ERR_TMA_TIMEOUT);
-                // let the copies in flight into the other stages land before leaving
-                for (int k = 1; k < STAGES; ++k) {
-                    const int j = i + k;
-                    if (blockIdx.x + j * G < ntiles)
-                        mbar_wait_bounded(bar + (j % STAGES), (unsigned)(j / STAGES) & 1u);
-                }
-            }
-            return;
-        }
-        const int x0 = (t % tiles_x) * AC_TX, z0 = (t / tiles_x) * T::TZ;
-        ac_tile_body<WARPS, RPW, SPONGE>(smem + st * T::FLOATS, g, s, x0, z0);
-        __syncthreads();  // every thread is done reading stage st
-        const int tn = blockIdx.x + (i + STAGES) * G;
-        if (tid == 0 && tn < ntiles) {
-            fence_proxy_async_shared();  // the generic reads of stage st before the async write
-            issue(tn, st);
-        }
-    }
-}
-
 // Launch with optional programmatic stream serialization (the kernel may begin
 // while the previous kernel of the stream drains).
 template <typename... KArgs, typename... Args>
@@ -642,54 +573,6 @@ inline cudaError_t launch_acoustic_persistent(const AcMaps& m, const AcGeom& g, 
                   tiles_x, ntiles);
     if (e == cudaSuccess) *base = b + (unsigned)(ntiles + grid);
     return e;
-}
-
-// Shared memory of the streaming form: STAGES stages and their barriers.
-template <int WARPS, int RPW, int SPONGE, int STAGES>
-constexpr size_t stream_smem_bytes()
-{
-    return STAGES * AcTile<WARPS, RPW, SPONGE>::FLOATS * 4u + 128;
-}
-
-// Resident CTAs of the streaming form on the current device (0 on error), one query per
-// instantiation and device.
-template <int WARPS, int RPW, int SPONGE, int STAGES>
-inline int stream_capacity()
-{
-    auto query = [](int dev) {
-        const int smem = (int)stream_smem_bytes<WARPS, RPW, SPONGE, STAGES>();
-        if (set_smem_once<acoustic_step_stream<WARPS, RPW, SPONGE, STAGES>>(smem) != cudaSuccess)
-            return 0;
-        int per_sm = 0, sms = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, acoustic_step_stream<WARPS, RPW, SPONGE, STAGES>, WARPS * 32, smem) !=
-                cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            return 0;
-        return per_sm * sms;
-    };
-    static std::once_flag once[W2D_MAX_DEVICES];
-    static int cap[W2D_MAX_DEVICES];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    if (dev < 0 || dev >= W2D_MAX_DEVICES) return query(dev);
-    std::call_once(once[dev], [&query, dev] { cap[dev] = query(dev); });
-    return cap[dev];
-}
-
-template <int WARPS, int RPW, int SPONGE, int STAGES>
-inline cudaError_t launch_acoustic_stream(const AcMaps& m, const AcGeom& g, const AcStep& s,
-                                          cudaStream_t st, int pdl)
-{
-    using T = AcTile<WARPS, RPW, SPONGE>;
-    const int cap = stream_capacity<WARPS, RPW, SPONGE, STAGES>();
-    if (cap <= 0) return cudaErrorInvalidConfiguration;
-    const int tiles_x = (g.nx + AC_TX - 1) / AC_TX;
-    const int ntiles = tiles_x * ((g.nz + T::TZ - 1) / T::TZ);
-    const int grid = cap < ntiles ? cap : ntiles;
-    return launch_ex(acoustic_step_stream<WARPS, RPW, SPONGE, STAGES>, dim3(grid),
-                     dim3(WARPS * 32), stream_smem_bytes<WARPS, RPW, SPONGE, STAGES>(), st, pdl,
-                     m, g, s, tiles_x, ntiles);
 }
 
 // Encode the TMA descriptors of one tile-step over pitched fields.

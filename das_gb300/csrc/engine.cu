@@ -44,10 +44,6 @@ template <int W, int R, int SP>
 static cudaError_t launch_one(const LaunchMode& lm, const AcMaps& m, const AcGeom& g,
                               const AcStep& s, cudaStream_t st)
 {
-    if constexpr ((W == 4 || W == 8) && R == 4) {
-        if (lm.persistent == 2) return launch_acoustic_stream<W, R, SP, 3>(m, g, s, st, lm.pdl);
-        if (lm.persistent == 3) return launch_acoustic_stream<W, R, SP, 2>(m, g, s, st, lm.pdl);
-    }
     if (lm.persistent)
         return launch_acoustic_persistent<W, R, SP>(m, g, s, st, lm.pdl, lm.counter, lm.base);
     return launch_acoustic_step<W, R, SP>(m, g, s, st, lm.pdl);
@@ -714,9 +710,8 @@ int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
 {
     W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
-    W2D_CHECK_ARG(persistent >= 0 && persistent <= 3, "launch mode must be 0..3");
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
-    e->persistent = persistent;
+    e->persistent = persistent ? 1 : 0;
     e->pdl = pdl ? 1 : 0;
     return W2D_OK;
 }

@@ -105,19 +105,15 @@ class WaveSolver2D:
             _lib.check(self._lib.w2d_engine_set_two_step(h, v))
         return h
 
-    _LAUNCH_KINDS = {"grid": 0, "persistent": 1, "stream": 2, "stream2": 3}
-
     def _apply_launch(self, h):
         kind, pdl = self.launch
-        if kind not in self._LAUNCH_KINDS:
-            raise ValueError(f"launch kind must be one of {sorted(self._LAUNCH_KINDS)}")
-        _lib.check(self._lib.w2d_engine_set_launch(h, self._LAUNCH_KINDS[kind], 1 if pdl else 0))
+        if kind not in ("grid", "persistent"):
+            raise ValueError("launch kind must be 'grid' or 'persistent'")
+        _lib.check(self._lib.w2d_engine_set_launch(h, 1 if kind == "persistent" else 0,
+                                                   1 if pdl else 0))
 
     def set_launch(self, kind: str = "grid", pdl: bool = True) -> None:
-        """Choose how the step kernels launch (results are identical in every mode):
-        "grid" one CTA per tile; "persistent" resident CTAs drawing tiles from a counter;
-        "stream" / "stream2" resident CTAs with a static share of the tiles streamed
-        through a 3- / 2-stage ring of TMA stages."""
+        """Choose how the step kernels launch (results are identical in every mode)."""
         self.launch = (kind, bool(pdl))
         if self._engine is not None:
             self._apply_launch(self._engine)

@@ -1,13 +1,10 @@
-"""Step launch modes: one CTA per tile, persistent CTAs over a tile counter, and
-resident CTAs streaming a static share of the tiles through a 3- or 2-stage TMA
-ring, each with or without programmatic dependent launch, give bit-identical
-results.
+"""Step launch modes: one CTA per tile or persistent CTAs over a tile counter, each
+with or without programmatic dependent launch, give bit-identical results.
 
 The persistent form draws tiles from a counter that is never reset between
 launches (each launch draws exactly ntiles + grid indices); long runs with
 checkpoint recomputation, forward and backward passes and many launches check
-that the accounting holds.  The streaming forms' rings wrap many times per launch
-on the 1000 x 1500 grid (more tiles than resident CTAs times stages).
+that the accounting holds.
 """
 import numpy as np
 import pytest
@@ -16,8 +13,7 @@ from oracle import oracle as o
 
 pytestmark = pytest.mark.gpu
 
-MODES = [("grid", False), ("persistent", False), ("persistent", True), ("stream", True),
-         ("stream", False), ("stream2", True)]
+MODES = [("grid", False), ("persistent", False), ("persistent", True)]
 
 
 def _solver(grid, tile, mode):
