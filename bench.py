@@ -119,13 +119,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, or None."""
+def committed_traffic(key="traffic_bytes_per_launch"):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary, or None:
+    `traffic_bytes_per_launch` in the live (warm-cache) regime, `cold_traffic_bytes_per_launch`
+    with the caches flushed before each launch."""
     p = os.path.join(REPO, "profiles", "acoustic_step_large_plain.md")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        m = re.search(r"(?m)^" + key + r":\s*([0-9.eE+]+)", f.read())
     return float(m.group(1)) if m else None
 
 
@@ -178,6 +180,25 @@ class Clocks:
         loaded = [r[0] for r in rows if r[2] > 200.0] or [r[0] for r in rows]
         return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(r[1] for r in rows),
                 "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# Clock sampler running around a whole non-default workload (its line carries the record
+# of the run; samples under load are those drawing more than 200 W).
+_WORKLOAD_CLOCKS = None
+
+
+def _emit(out: dict) -> None:
+    """Print a workload's JSON line with the clock record of its run."""
+    if _WORKLOAD_CLOCKS is not None:
+        out["clocks"] = _WORKLOAD_CLOCKS.stop()
+    print(json.dumps(out), flush=True)
+
+
+def _gpu_bus_id(local: int) -> str:
+    import das_gb300
+    lib = das_gb300.lib()
+    bus = ctypes.create_string_buffer(64)
+    return bus.value.decode() if lib.w2d_device_pci_bus_id(bus, 64) == 0 else str(local)
 
 
 # ------------------------------------------------------------------------------ workload
@@ -443,6 +464,13 @@ def run_ours(args, dist):
                "device_memory_in_use_gb": (total_b - free_b) / 1e9,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic,
+                            "traffic_cold": committed_traffic("cold_traffic_bytes_per_launch"),
+                            "limiter": "latency: the three wave planes and the model (64 MB) "
+                                       "stay in L2 from step to step, so DRAM carries the "
+                                       "snapshot stream and write-backs (traffic: warm-cache "
+                                       "ncu, per launch) and each CTA waits on its own TMA "
+                                       "round trip; frac is algorithmic bytes over the HBM "
+                                       "copy rate",
                             "peak_source": f"{peak_kind} hbm_gbs",
                             "kernel": "acoustic_step_kernel (fused forward / backward+imaging)",
                             "algorithmic_bytes_per_launch": per_launch},
@@ -569,7 +597,7 @@ def run_batched(args, dist):
     out["roofline"] = {"bound": "hbm", "achieved": dev, "peak": peak, "unit": "GB/s",
                        "frac": dev / peak, "peak_source": f"{peak_kind} hbm_gbs",
                        "kernel": "acoustic_batch_step_kernel", "bytes_per_counted_point": 22.0}
-    print(json.dumps(out), flush=True)
+    _emit(out)
 
 
 def _served_trace(n_jobs, rate, seed, side_scale=1.0, nt_scale=1.0):
@@ -689,7 +717,7 @@ def run_elastic(args, dist):
                         "algorithmic_bytes_per_step_point": 56 + 20 + 168,
                         "forward_phase_achieved_gbs": fwd_achieved,
                         "forward_phase_frac": fwd_achieved / peak}}
-    print(json.dumps(out), flush=True)
+    _emit(out)
 
 
 def run_served(args, dist):
@@ -780,7 +808,7 @@ def run_served(args, dist):
                       f"nt={min(args.cpu_nt, len(ac[0].shots[0].wavelet))}: {rate:.2f} Gpts/s in "
                       f"{el:.1f} s, extrapolated to the trace's {n_ac} acoustic shots "
                       f"({ac_pts / 1e12:.2f} T counted points)"}
-    print(json.dumps(out_line), flush=True)
+    _emit(out_line)
 
 
 def run_interferometry(args, dist):
@@ -848,7 +876,7 @@ def run_interferometry(args, dist):
                             "kind": "port", "sample": f"{k} windows, numpy FFT (float32)"}}
     st.close()
     st2.close()
-    print(json.dumps(out), flush=True)
+    _emit(out)
 
 
 def run_small(args, dist):
@@ -918,7 +946,7 @@ def run_small(args, dist):
            "shots_per_s": n / timing["auto"], "shots_per_s_per_shot_loop": n / timing["off"],
            "batched_equals_per_shot_loop": same, "cpu_baseline": cpu}
     solver.close()
-    print(json.dumps(out), flush=True)
+    _emit(out)
 
 
 def main():
@@ -977,6 +1005,10 @@ def main():
         torch.cuda.set_device(local)
         _lib.check(_lib.load().w2d_set_device(local))  # handles made on this thread bind here
     dist = Dist("nccl" if world > 1 else "gloo")
+    global _WORKLOAD_CLOCKS
+    if args.workload != "large":
+        _WORKLOAD_CLOCKS = Clocks(_gpu_bus_id(local), rank)
+        _WORKLOAD_CLOCKS.start()
     try:
         if args.workload == "batched":
             run_batched(args, dist)
@@ -991,6 +1023,9 @@ def main():
         else:
             run_ours(args, dist)
     finally:
+        c = _WORKLOAD_CLOCKS
+        if c is not None and c.proc is not None and c.proc.poll() is None:
+            c.stop()  # a workload that failed before its line: end the sampler
         dist.close()
 
 
