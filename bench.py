@@ -351,6 +351,7 @@ def run_ours(args, dist):
         solver.tile = tuple(int(t) for t in args.tile.split(","))
     solver.l2_hints = bool(args.l2_hints)
     solver.set_launch(args.launch, bool(args.pdl))
+    solver.set_graphs(bool(args.graphs))
     eng = solver._eng()
     K, W = args.steps, args.warmup
     n_sh = K + W
@@ -458,6 +459,7 @@ def run_ours(args, dist):
                           "shots_per_step": 1, "snapshot_interval": interval,
                           "storage": used, "tile": list(solver.tile or (4, 4)),
                           "launch": args.launch, "pdl": bool(args.pdl),
+                          "graphs": bool(args.graphs),
                           "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
                "shots_per_s": K * dist.world / dev_s,
                "recomputed_steps_per_shot": recompute / max(K, 1),
@@ -962,6 +964,7 @@ def main():
     ap.add_argument("--l2-hints", type=int, default=0)
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
     ap.add_argument("--pdl", type=int, default=1)
+    ap.add_argument("--graphs", type=int, default=1)
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)

@@ -51,6 +51,7 @@ _SIGS = {
     "w2d_engine_set_l2_hints": (c_int, [c_void_p, c_int]),
     "w2d_engine_set_launch": (c_int, [c_void_p, c_int, c_int]),
     "w2d_engine_set_two_step": (c_int, [c_void_p, c_int]),
+    "w2d_engine_set_graphs": (c_int, [c_void_p, c_int]),
     "w2d_forward": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int,
                             c_void_p, c_void_p, c_int]),
     "w2d_backward_correlate": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_int, c_int,

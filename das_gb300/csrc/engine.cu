@@ -172,6 +172,26 @@ struct w2d_engine {
 
     struct w2d_fwi_state* fwi = nullptr;  // differentiable-path state (checkpoints, gradient)
 
+    // A migration's forward pass and backward pass, each captured once as a CUDA graph
+    // and replayed for every later shot with the same launch sequence (the key: sizes,
+    // modes, tile and every buffer address the launches hold).  One graph launch per
+    // pass instead of one host launch per step: no host stall can drain the stream
+    // between steps.  Default launch mode only (the two-step and counter modes carry
+    // host-side state from launch to launch).
+    struct PassGraph {
+        std::vector<uintptr_t> key;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0, recompute = 0;
+        void reset()
+        {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            key.clear();
+        }
+    };
+    PassGraph g_fwd, g_bwd;
+    int use_graphs = 1;
+
     float* wave(int i) { return waves.p + (size_t)perm[i] * plane; }  // logical plane i
     float* phys(int k) { return waves.p + (size_t)k * plane; }
     const CUtensorMap& mcurr(int i) const { return map_curr[perm[i]]; }
@@ -669,6 +689,8 @@ void w2d_engine_destroy(w2d_engine* e)
     W2D_ON_DEVICE_OF(e);
     if (!e) return;
     if (e->stream) cudaStreamSynchronize(e->stream);
+    e->g_fwd.reset();
+    e->g_bwd.reset();
     for (DevBuf<float>* b : {&e->sponge_lut, &e->sponge_arr, &e->waves, &e->v2dt2, &e->staging,
                              &e->wavelet, &e->data, &e->rec_out, &e->snaps, &e->ckpt, &e->image,
                              &e->illum, &e->stack_img, &e->stack_ill})
@@ -713,6 +735,17 @@ int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
     e->persistent = persistent ? 1 : 0;
     e->pdl = pdl ? 1 : 0;
+    return W2D_OK;
+}
+
+int w2d_engine_set_graphs(w2d_engine* e, int on)
+{
+    W2D_ON_DEVICE_OF(e);
+    W2D_CHECK_ARG(e, "engine is NULL");
+    W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->use_graphs = on ? 1 : 0;
+    e->g_fwd.reset();
+    e->g_bwd.reset();
     return W2D_OK;
 }
 
@@ -876,6 +909,69 @@ namespace {
 
 // Forward + backward migration of one shot whose wavelet and data are already
 // on the device (e->cur_w, e->cur_data) and whose geometry is set.
+// Everything a pass's launches hold: when it matches a cached graph, replaying the
+// graph issues exactly the launches the host code would.
+std::vector<uintptr_t> pass_key(const w2d_engine* e, int pass, int nt, int interval, int mode,
+                                int seg, int n_rec)
+{
+    std::vector<uintptr_t> k = {
+        (uintptr_t)pass, (uintptr_t)nt, (uintptr_t)interval, (uintptr_t)mode, (uintptr_t)seg,
+        (uintptr_t)n_rec, (uintptr_t)e->tile.warps, (uintptr_t)e->tile.rpw, (uintptr_t)e->pdl,
+        (uintptr_t)e->l2_hints, (uintptr_t)e->use_lut, (uintptr_t)e->use_arr,
+        (uintptr_t)e->tm_tz, (uintptr_t)e->waves.p, (uintptr_t)e->snaps.p, (uintptr_t)e->ckpt.p,
+        (uintptr_t)e->v2dt2.p, (uintptr_t)e->image.p, (uintptr_t)e->illum.p,
+        (uintptr_t)e->cur_w, (uintptr_t)e->cur_data, (uintptr_t)e->rec_ptr.p,
+        (uintptr_t)e->rec_list.p, (uintptr_t)e->shot.p, (uintptr_t)e->err.p,
+        (uintptr_t)e->sponge_lut.p, (uintptr_t)e->sponge_arr.p};
+    for (int i = 0; i < 6; ++i) k.push_back((uintptr_t)e->perm[i]);
+    return k;
+}
+
+// Run one pass: replay its cached graph when the key matches, else capture the pass
+// from `body` (the host code that launches it), instantiate and launch the graph.  With
+// graphs off, or in a launch mode that keeps host-side state, `body` runs directly.  A
+// capture the runtime refuses turns graphs off for this engine and runs `body`.
+template <typename F>
+int run_pass(w2d_engine* e, w2d_engine::PassGraph& pg, std::vector<uintptr_t> key, F&& body)
+{
+    if (!e->use_graphs || e->two_step || e->persistent) return body();
+    if (pg.exec && pg.key == key) {
+        W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
+        e->last_launches += pg.launches;
+        e->last_recompute += pg.recompute;
+        return W2D_OK;
+    }
+    pg.reset();
+    const long long l0 = e->last_launches, r0 = e->last_recompute;
+    W2D_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = body();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+    if (rc || ce != cudaSuccess || !graph) {
+        // Nothing captured has run.  Whatever refused the capture (the pass's own
+        // launches are checked again below), run this and later passes as direct
+        // launches on this engine.
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        e->use_graphs = 0;
+        e->last_launches = l0;
+        e->last_recompute = r0;
+        return body();
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&pg.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        pg.exec = nullptr;
+        set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+        return W2D_ECUDA;
+    }
+    pg.key = std::move(key);
+    pg.launches = e->last_launches - l0;
+    pg.recompute = e->last_recompute - r0;
+    W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
+    return W2D_OK;
+}
+
 int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int storage,
                  float* image_out, float* illum_out)
 {
@@ -919,40 +1015,47 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
     const float dt2inj = (float)(e->dt_d * e->dt_d);
     const float img_dt = (float)(e->dt_d * (double)interval);
     cudaEventRecord(e->ev0, e->stream);
-    W2D_CUDA_TRY(cudaMemsetAsync(e->illum.p, 0, plane_b, e->stream));
-    W2D_CUDA_TRY(cudaMemsetAsync(e->image.p, 0, plane_b, e->stream));
 
     // 1. forward pass in slot 0 with illumination
-    if ((rc = forward_begin(e, dt2inj))) return rc;
-    FwdOpts o;
-    o.nt = nt;
-    o.interval = interval;
-    o.illum = true;
-    if (mode == W2D_STORE_ALL) {
-        o.snaps = e->snaps.p;
-    } else {
-        o.ckpt = e->ckpt.p;
-        o.ckpt_every = seg;
-    }
-    if ((rc = run_forward_steps(e, 0, o, 0, nt, 0.0, dt2inj))) return rc;
-    scale_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->illum.p, e->plane, img_dt);
-    e->last_launches++;
+    auto forward = [&]() -> int {
+        int r;
+        W2D_CUDA_TRY(cudaMemsetAsync(e->illum.p, 0, plane_b, e->stream));
+        W2D_CUDA_TRY(cudaMemsetAsync(e->image.p, 0, plane_b, e->stream));
+        if ((r = forward_begin(e, dt2inj))) return r;
+        FwdOpts o;
+        o.nt = nt;
+        o.interval = interval;
+        o.illum = true;
+        if (mode == W2D_STORE_ALL) {
+            o.snaps = e->snaps.p;
+        } else {
+            o.ckpt = e->ckpt.p;
+            o.ckpt_every = seg;
+        }
+        if ((r = run_forward_steps(e, 0, o, 0, nt, 0.0, dt2inj))) return r;
+        scale_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->illum.p, e->plane, img_dt);
+        e->last_launches++;
+        W2D_CUDA_TRY(cudaGetLastError());
+        return W2D_OK;
+    };
+    if ((rc = run_pass(e, e->g_fwd, pass_key(e, 0, nt, interval, mode, seg, n_rec), forward)))
+        return rc;
 
     // 2. backward pass in slot 1 with imaging
     if (e->data_pending) {  // the receiver data uploaded beside the forward pass
         W2D_CUDA_TRY(cudaStreamWaitEvent(e->stream, e->data_ready, 0));
         e->data_pending = false;
     }
-    if (n_rec > 0) {
-        if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
-    } else {
-        if ((rc = zero_pass(e, 1))) return rc;
-    }
-    if (mode == W2D_STORE_ALL) {
-        if ((rc = run_backward_steps(e, 1, nt, interval, n_rec, nt - 1, 0, e->snaps.p, 0, n_snaps,
-                                     img_dt, dt2inj)))
-            return rc;
-    } else {
+    auto backward = [&]() -> int {
+        int rb;
+        if (n_rec > 0) {
+            if ((rb = backward_begin(e, nt, n_rec, dt2inj))) return rb;
+        } else {
+            if ((rb = zero_pass(e, 1))) return rb;
+        }
+        if (mode == W2D_STORE_ALL)
+            return run_backward_steps(e, 1, nt, interval, n_rec, nt - 1, 0, e->snaps.p, 0,
+                                      n_snaps, img_dt, dt2inj);
         for (int sgi = n_seg - 1; sgi >= 0; --sgi) {
             const int a = sgi * seg, b = std::min(nt, a + seg);
             // restore the forward state at step a and recompute [a, b) with snapshots
@@ -968,13 +1071,17 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
             r.interval = interval;
             r.snaps = e->snaps.p;
             r.slot0 = (a + interval - 1) / interval;  // first snapshot index in [a, b)
-            if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
+            int q;
+            if ((q = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return q;
             e->last_recompute += b - a;
-            if ((rc = run_backward_steps(e, 1, nt, interval, n_rec, b - 1, a, e->snaps.p, r.slot0,
-                                         n_snaps, img_dt, dt2inj)))
-                return rc;
+            if ((q = run_backward_steps(e, 1, nt, interval, n_rec, b - 1, a, e->snaps.p, r.slot0,
+                                        n_snaps, img_dt, dt2inj)))
+                return q;
         }
-    }
+        return W2D_OK;
+    };
+    if ((rc = run_pass(e, e->g_bwd, pass_key(e, 1, nt, interval, mode, seg, n_rec), backward)))
+        return rc;
     cudaEventRecord(e->ev1, e->stream);
     if (image_out) {
         if ((rc = download_field(e, image_out, e->image.p)) ||
@@ -1087,8 +1194,18 @@ int w2d_migrate_staged(w2d_engine* e, int slot, int src_ix, int src_iz, const in
                              illum_out)))
         return rc;
     if ((rc = set_shot(e, src_ix, src_iz, rec_ix, n_rec, rec_iz))) return rc;
-    e->cur_w = e->st_w[slot].p;
-    e->cur_data = e->st_d[slot].p;
+    // the staged inputs move into the engine's own input buffers (a device-to-device copy
+    // of a few hundred microseconds at most), so every shot's passes hold the same
+    // addresses and replay the same captured graphs
+    if ((rc = e->wavelet.ensure(nt)) || (rc = e->data.ensure((size_t)nt * std::max(n_rec, 1))))
+        return rc;
+    W2D_CUDA_TRY(cudaMemcpyAsync(e->wavelet.p, e->st_w[slot].p, (size_t)nt * 4,
+                                 cudaMemcpyDeviceToDevice, e->stream));
+    if (n_rec > 0)
+        W2D_CUDA_TRY(cudaMemcpyAsync(e->data.p, e->st_d[slot].p, (size_t)nt * n_rec * 4,
+                                     cudaMemcpyDeviceToDevice, e->stream));
+    e->cur_w = e->wavelet.p;
+    e->cur_data = e->data.p;
     return migrate_core(e, nt, n_rec, snapshot_interval, storage, image_out, illum_out);
 }
 

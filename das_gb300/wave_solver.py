@@ -74,6 +74,7 @@ class WaveSolver2D:
         # each optionally a programmatic dependent of the previous step (pdl)
         self.launch = ("grid", True)
         self.two_step = False  # two time steps per launch (grid launch mode; off by default)
+        self.graphs = True  # migrations replay each pass as a captured CUDA graph
 
     def _default_sponge(self) -> np.ndarray:
         """The Cerjan sponge of this grid's (n_sponge, sponge_alpha) as built at creation."""
@@ -103,7 +104,16 @@ class WaveSolver2D:
         if self.two_step is not False:
             v = 1 if self.two_step is True else int(self.two_step)
             _lib.check(self._lib.w2d_engine_set_two_step(h, v))
+        if not self.graphs:
+            _lib.check(self._lib.w2d_engine_set_graphs(h, 0))
         return h
+
+    def set_graphs(self, on: bool = True) -> None:
+        """Replay each migration pass as a captured CUDA graph (True, the default) or
+        launch every step from the host (False).  Results are identical."""
+        self.graphs = bool(on)
+        if self._engine is not None:
+            _lib.check(self._lib.w2d_engine_set_graphs(self._engine, 1 if on else 0))
 
     def _apply_launch(self, h):
         kind, pdl = self.launch

@@ -108,6 +108,13 @@ int w2d_engine_set_l2_hints(w2d_engine* e, int on);
  * launches each step as a programmatic dependent of the previous one, so its
  * set-up overlaps the previous step's tail.  Default: persistent 0, pdl 1. */
 int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl);
+/* CUDA graphs for migrations (on = 1, the default): the forward pass and the backward
+ * pass of w2d_migrate_shot / w2d_migrate_staged are each captured once as a graph and
+ * replayed for later shots with the same sizes, modes and buffers, one graph launch
+ * per pass instead of one host launch per step (default launch mode only; the
+ * two-step and counter modes launch directly).  Bit-identical either way.  on = 0
+ * launches every step from the host and drops the cached graphs. */
+int w2d_engine_set_graphs(w2d_engine* e, int on);
 /* Two time steps per launch (one-CTA-per-tile mode only): each 128 x (4 *
  * rows_per_warp) tile evaluates step n on itself plus a 2-cell ring in shared memory,
  * then step n+1, so every wavefield crosses memory once per two steps; bit-identical

@@ -112,3 +112,43 @@ def test_two_step_equals_one_step(fs, custom_sponge, rows):
     for a, b in zip(out[rows], out[False]):
         np.testing.assert_array_equal(a, b)
     assert np.abs(out[rows][2]).max() > 0
+
+
+@pytest.mark.parametrize("storage", ["all", "checkpoint"])
+def test_graph_replays_equal_direct_launches(storage):
+    """Migrations replaying captured pass graphs (the default) equal migrations whose
+    steps are launched one by one from the host, bit for bit, over a sequence of shots:
+    the first shot captures, later shots with new sources, receivers' data and models
+    replay the cached graphs, a shorter shot captures again, and the step counts the
+    engine reports are the same."""
+    from das_gb300.rtm_engine import TSWRTMEngine
+    from das_gb300.velocity_flood import FloodModels
+    from das_gb300.wave_solver import WaveSolver2D
+    nz, nx = 180, 700
+    rng = np.random.default_rng(5)
+    grid = o.Grid(nx, nz, 5.0, 5.0, 5e-4, 30, 0.0015, True)
+    w, _ = o.ricker_wavelet(12.0, grid.dt, 0.12)
+    rix = np.arange(3, nx - 3, 3)
+    shots = []
+    for k, (six, nt) in enumerate([(100, len(w)), (350, len(w)), (620, len(w)), (40, len(w) - 37),
+                                   (500, len(w))]):
+        v = rng.uniform(1600, 3000, (nz, nx)).astype(np.float32)
+        d = (rng.standard_normal((nt, len(rix))) * 1e-6).astype(np.float32)
+        shots.append((FloodModels(v, v, (v * 1.01).astype(np.float32), 0, 0), w[:nt], six, d))
+    out = {}
+    for graphs in (True, False):
+        s = WaveSolver2D(nx, nz, 5.0, 5.0, grid.dt, 30, 0.0015, True)
+        s.set_graphs(graphs)
+        eng = TSWRTMEngine(s, storage=storage)
+        res = []
+        for fm, wk, six, d in shots:
+            img, ill = eng.migrate_shot(fm, wk, six, 2, d, rix, 2, 2)
+            st = s.last_stats()
+            res.append((img, ill, st["step_launches"], st["recomputed_steps"], st["storage"]))
+        out[graphs] = res
+        s.close()
+    for k, (a, b) in enumerate(zip(out[True], out[False])):
+        np.testing.assert_array_equal(a[0], b[0], err_msg=f"image, shot {k}")
+        np.testing.assert_array_equal(a[1], b[1], err_msg=f"illumination, shot {k}")
+        assert a[2:] == b[2:] and a[4] == storage, (k, a[2:], b[2:])
+        assert np.abs(a[0]).max() > 0
