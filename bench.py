@@ -962,7 +962,7 @@ def main():
     ap.add_argument("--el-tiles", default="4,2:4,1")  # step warps,rows : adjoint warps,rows
     ap.add_argument("--small-cpu-shots", type=int, default=20)
     ap.add_argument("--l2-hints", type=int, default=0)
-    ap.add_argument("--launch", default="grid", choices=["grid", "persistent", "coop"])
+    ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
     ap.add_argument("--pdl", type=int, default=1)
     ap.add_argument("--graphs", type=int, default=1)
     ap.add_argument("--serve-jobs", type=int, default=40)

@@ -485,167 +485,6 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
-// ---------------------------------------------------------------------------------
-// Time-persistent form: one cooperative launch advances S consecutive steps of a pass.
-//
-// Each resident CTA owns a static set of tiles (CTA b: tiles b, b + G, b + 2G, ...) and
-// walks them in step order: all of its tiles at step j, then at step j + 1.  A tile
-// starts step j once its 3 x 3 neighbour tiles have published step j - 1 (per-tile
-// counters `done`, st.release after the tile's stores, ld.acquire before the halo box is
-// loaded), so there is no launch, grid-wide barrier or memory flush between steps.  The
-// p_prev and v^2 dt^2 boxes read only what this tile itself wrote (or the model) and are
-// issued before the wait; only the p_curr box, whose halo neighbours wrote, waits.
-//
-// Why the neighbour dependency suffices: step j writes p_next into the plane that held
-// the field of step j - 2 (p_curr at step j - 2, read by the 3 x 3 neighbourhood through
-// the halo; p_prev at step j - 1, read by the tile itself), and reads what the
-// neighbourhood wrote at step j - 1.  Why it cannot deadlock: all CTAs are resident
-// (cooperative launch), each walks its tiles in step order, so every tile-step a CTA
-// waits for belongs to an earlier step of a CTA that reaches it.  Every wait is bounded;
-// a timeout sets ERR_DEP_TIMEOUT | ERR_ABORT and all CTAs stop.  The tile body is the
-// one every other form runs: results are bit-identical to one launch per step.
-struct AcPlan {
-    AcMaps maps[3];      // TMA descriptors of local step j use maps[j % 3]
-    float* next[3];      // and p_next = next[j % 3]
-    int dir;             // +1 forward pass (it = it0 + j), -1 backward pass (it = it0 - j)
-    int it0, S;          // reference step of local step 0; steps in this launch
-    int nt, interval, n_rec;
-    unsigned j0;         // steps of this sequence completed before the launch
-    int tiles_x, tiles_z, ntiles;
-    size_t plane;        // floats per pitched plane
-    float dt2_inj, img_dt;
-    // forward pass
-    const float* wavelet;  // source sample of step it + 1 injected by step it
-    float* rec_out;        // (nt, n_rec) samples of p_next, or null
-    float* snaps;          // snapshot it / interval - slot0 on it % interval == 0, or null
-    float* illum;          // += p_curr^2 on snapshot steps, or null
-    // backward pass
-    const float* data;     // receiver row it - 1 injected by step it, or null
-    const float* snap_in;  // forward snapshot k - slot0 of imaging steps, or null
-    float* image;
-    int slot0, n_snaps_valid;
-    unsigned* done;        // per tile: steps of this sequence completed
-    unsigned* err;
-};
-
-// Bounded wait until *p >= target (acquire).  Gives up early when another CTA has set
-// ERR_ABORT; on timeout sets ERR_DEP_TIMEOUT | ERR_ABORT so that every CTA stops.
-__device__ __forceinline__ bool wait_done(const unsigned* p, unsigned target, unsigned* err)
-{
-    for (unsigned i = 0; i < (1u << 24); ++i) {
-        if (ld_acquire_u32(p) >= target) return true;
-        if (i > 64) __nanosleep(128);
-        if ((i & 1023) == 1023 && (*reinterpret_cast<volatile unsigned*>(err) & ERR_ABORT))
-            return false;
-    }
-    atomicOr(err, ERR_DEP_TIMEOUT | ERR_ABORT);
-    return false;
-}
-
-// The AcStep of local step j (the per-step options of the host loops, step for step).
-__device__ __forceinline__ void ac_plan_step(const AcPlan& p, int j, AcStep& s)
-{
-    const int it = p.it0 + p.dir * j;
-    s.p_next = p.next[j % 3];
-    s.snap_out = nullptr;
-    s.illum = nullptr;
-    s.rec_out = nullptr;
-    s.snap_in = nullptr;
-    s.image = nullptr;
-    s.img_dt = p.img_dt;
-    s.inj_w = nullptr;
-    s.inj_data = nullptr;
-    s.dt2_inj = p.dt2_inj;
-    s.err = p.err;
-    if (p.dir > 0) {
-        if (it + 1 < p.nt) s.inj_w = p.wavelet + it + 1;
-        if (p.rec_out) s.rec_out = p.rec_out + (size_t)it * p.n_rec;
-        if (it % p.interval == 0) {
-            if (p.snaps) s.snap_out = p.snaps + (size_t)(it / p.interval - p.slot0) * p.plane;
-            if (p.illum) s.illum = p.illum;
-        }
-    } else {
-        if (it >= 1 && p.n_rec > 0 && p.data) s.inj_data = p.data + (size_t)(it - 1) * p.n_rec;
-        if (p.snap_in && it % p.interval == 0) {
-            const int k = it / p.interval;
-            if (k >= 0 && k < p.n_snaps_valid) {
-                s.snap_in = p.snap_in + (size_t)(k - p.slot0) * p.plane;
-                s.image = p.image;
-            }
-        }
-    }
-}
-
-// Registers held to what the shared memory allows resident: 8 CTAs of a 128 x 16 tile,
-// 4 of a 128 x 32 tile per SM.
-template <int WARPS, int RPW, int SPONGE>
-__global__ void __launch_bounds__(WARPS * 32, 128 / (WARPS * RPW))
-    acoustic_steps_coop(const __grid_constant__ AcPlan p, const AcGeom g)
-{
-    using T = AcTile<WARPS, RPW, SPONGE>;
-    extern __shared__ __align__(128) float smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
-    __shared__ int s_ok;
-    const int tid = threadIdx.x;
-    const int G = gridDim.x;
-    if (tid == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-        s_ok = 1;
-    }
-    __syncthreads();
-    unsigned phase = 0;
-    for (int j = 0; j < p.S; ++j) {
-        AcStep s;
-        ac_plan_step(p, j, s);
-        const AcMaps& m = p.maps[j % 3];
-        const unsigned need = p.j0 + (unsigned)j;  // neighbours have completed step j - 1
-        for (int t = blockIdx.x; t < p.ntiles; t += G) {
-            const int tx = t % p.tiles_x, tz = t / p.tiles_x;
-            const int x0 = tx * AC_TX, z0 = tz * T::TZ;
-            if (tid == 0) {
-                // this tile's own planes: what it wrote before (ordered by the barrier
-                // that ended its previous tile-step) and the model
-                fence_proxy_async_global();
-                fence_proxy_async_shared();
-                mbar_expect_tx(bar, T::TX_BYTES);
-                tma_load_2d(smem + T::C_FLOATS, &m.prev, x0, z0, bar);
-                tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &m.vel, x0, z0, bar);
-                if (SPONGE == SPONGE_ARRAY)
-                    tma_load_2d(smem + T::C_FLOATS + 2 * T::P_FLOATS, &m.sponge, x0, z0, bar);
-            }
-            if (s.snap_in && tid < T::TZ && z0 + tid < g.nz)
-                prefetch_l2_bulk(s.snap_in + (size_t)(z0 + tid) * g.ldx + x0,
-                                 (uint32_t)min(AC_TX, g.ldx - x0) * 4u);
-            if (tid < 9 && need > 0) {
-                const int ux = tx + tid % 3 - 1, uz = tz + tid / 3 - 1;
-                if (ux >= 0 && ux < p.tiles_x && uz >= 0 && uz < p.tiles_z)
-                    if (!wait_done(p.done + uz * p.tiles_x + ux, need, p.err)) s_ok = 0;
-            }
-            __syncthreads();
-            const int ok = s_ok;
-            if (tid == 0) {
-                // issued also when a wait failed (the CTA then discards the box): the
-                // barrier completes and no copy lands after the CTA has left
-                fence_proxy_async_global();  // the neighbours' stores, acquired above
-                tma_load_2d(smem, &m.curr, x0 - AC_HX, z0 - 2, bar);
-            }
-            const bool got = mbar_wait_bounded(bar, phase);
-            phase ^= 1u;
-            if (__syncthreads_or(!got || !ok)) {
-                if (tid == 0 && !got) atomicOr(p.err, ERR_TMA_TIMEOUT | ERR_ABORT);
-                return;
-            }
-            ac_tile_body<WARPS, RPW, SPONGE>(smem, g, s, x0, z0);
-            __syncthreads();
-            if (tid == 0) {
-                __threadfence();
-                st_release_u32(p.done + t, need + 1u);
-            }
-        }
-    }
-}
-
 // Launch with optional programmatic stream serialization (the kernel may begin
 // while the previous kernel of the stream drains).
 template <typename... KArgs, typename... Args>
@@ -734,55 +573,6 @@ inline cudaError_t launch_acoustic_persistent(const AcMaps& m, const AcGeom& g, 
                   tiles_x, ntiles);
     if (e == cudaSuccess) *base = b + (unsigned)(ntiles + grid);
     return e;
-}
-
-// Resident CTAs of the time-persistent form on the current device (0 on error): the
-// cooperative launch requires the whole grid to be resident at once.
-template <int WARPS, int RPW, int SPONGE>
-inline int coop_capacity()
-{
-    auto query = [](int dev) {
-        using T = AcTile<WARPS, RPW, SPONGE>;
-        if (set_smem_once<acoustic_steps_coop<WARPS, RPW, SPONGE>>((int)T::SMEM_BYTES) !=
-            cudaSuccess)
-            return 0;
-        int per_sm = 0, sms = 0, coop = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, acoustic_steps_coop<WARPS, RPW, SPONGE>, WARPS * 32,
-                (int)T::SMEM_BYTES) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
-            !coop)
-            return 0;
-        return per_sm * sms;
-    };
-    static std::once_flag once[W2D_MAX_DEVICES];
-    static int cap[W2D_MAX_DEVICES];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    if (dev < 0 || dev >= W2D_MAX_DEVICES) return query(dev);
-    std::call_once(once[dev], [&query, dev] { cap[dev] = query(dev); });
-    return cap[dev];
-}
-
-// One cooperative launch of the time-persistent form over p.S steps.
-template <int WARPS, int RPW, int SPONGE>
-inline cudaError_t launch_acoustic_coop(const AcPlan& p, const AcGeom& g, cudaStream_t st)
-{
-    using T = AcTile<WARPS, RPW, SPONGE>;
-    const int cap = coop_capacity<WARPS, RPW, SPONGE>();
-    if (cap <= 0) return cudaErrorCooperativeLaunchTooLarge;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cap < p.ntiles ? cap : p.ntiles);
-    cfg.blockDim = dim3(WARPS * 32);
-    cfg.dynamicSmemBytes = T::SMEM_BYTES;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, acoustic_steps_coop<WARPS, RPW, SPONGE>, p, g);
 }
 
 // Encode the TMA descriptors of one tile-step over pitched fields.

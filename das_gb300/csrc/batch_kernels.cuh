@@ -69,6 +69,18 @@ struct BatchArgs {
     unsigned* err;
 };
 
+__device__ __forceinline__ bool wait_counter(const unsigned* p, unsigned target, unsigned* err)
+{
+    for (unsigned i = 0; i < (1u << 24); ++i) {
+        if (ld_acquire_u32(p) >= target) return true;
+        if (i > 64) __nanosleep(128);
+        if ((i & 1023) == 1023 && (*reinterpret_cast<volatile unsigned*>(err) & ERR_ABORT))
+            return false;
+    }
+    atomicOr(err, ERR_DEP_TIMEOUT | ERR_ABORT);
+    return false;
+}
+
 // The AcStep and TMA-descriptor indices of phase step k of one shot.
 __device__ __forceinline__ void batch_phase(const BShot* sh, int k, unsigned* err, AcStep& s,
                                             int& ci, int& pi, int& vi)
@@ -163,7 +175,7 @@ __global__ void __launch_bounds__(WARPS * 32, RPW == 4 ? 1024 / (WARPS * 32) : 1
         if (tid < 9 && k > 0) {
             const int nx_ = tx + tid % 3 - 1, nz_ = tz + tid / 3 - 1;
             if (nx_ >= 0 && nx_ < tiles_x && nz_ >= 0 && nz_ < tiles_z)
-                if (!wait_done(sh->done + nz_ * tiles_x + nx_, (unsigned)k, a.err)) s_ok = 0;
+                if (!wait_counter(sh->done + nz_ * tiles_x + nx_, (unsigned)k, a.err)) s_ok = 0;
         }
         __syncthreads();
         if (!s_ok) break;

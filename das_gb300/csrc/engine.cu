@@ -116,7 +116,6 @@ struct w2d_engine {
     bool chain = false;  // the last operation on the stream is a step kernel launched by step()
     DevBuf<unsigned> tile_counter;
     unsigned counter_base = 0;
-    DevBuf<unsigned> coop_done;  // time-persistent mode: per tile, steps completed
 
     int n_sponge = 0;
     DevBuf<float> sponge_lut, sponge_arr;
@@ -422,86 +421,6 @@ struct FwdOpts {
     int ckpt_every = 0;
 };
 
-// ---- time-persistent launches (launch mode 2) ------------------------------------
-// Steps per cooperative launch: a launch boundary costs one kernel's ramp, so few and long.
-constexpr int COOP_CHUNK = 2048;
-
-bool coop_mode(const w2d_engine* e)
-{
-    return e->persistent == 2 && !e->two_step && e->tile.rpw == 4 &&
-           (e->tile.warps == 4 || e->tile.warps == 8);
-}
-
-int coop_tiles(const w2d_engine* e, int* tx, int* tz)
-{
-    *tx = (e->nx + AC_TX - 1) / AC_TX;
-    *tz = (e->nz + e->tile.tz() - 1) / e->tile.tz();
-    return *tx * *tz;
-}
-
-// A fresh step sequence: every tile has completed 0 steps of it.
-int coop_begin(w2d_engine* e)
-{
-    int tx, tz;
-    const int n = coop_tiles(e, &tx, &tz);
-    int rc;
-    if ((rc = e->coop_done.ensure(n))) return rc;
-    W2D_CUDA_TRY(cudaMemsetAsync(e->coop_done.p, 0, (size_t)n * 4, e->stream));
-    return W2D_OK;
-}
-
-AcPlan coop_plan(w2d_engine* e, int dir, int it0, int S, int nt, int interval, int n_rec,
-                 unsigned j0, int slot, float dt2inj_f)
-{
-    AcPlan p;
-    memset(&p, 0, sizeof p);
-    for (int r = 0; r < 3; ++r) {
-        const int it = it0 + dir * r;
-        int curr, prev, next;
-        if (dir > 0) {
-            curr = (it + 1) % 3;
-            prev = it % 3;
-            next = (it + 2) % 3;
-        } else {
-            const int m = nt - 1 - it;
-            curr = 3 + (m + 1) % 3;
-            prev = 3 + m % 3;
-            next = 3 + (m + 2) % 3;
-        }
-        p.maps[r].curr = e->mcurr(curr);
-        p.maps[r].prev = e->mprev(prev);
-        p.maps[r].vel = e->map_vel[slot];
-        p.maps[r].sponge = e->map_sponge;
-        p.next[r] = e->wave(next);
-    }
-    p.dir = dir;
-    p.it0 = it0;
-    p.S = S;
-    p.nt = nt;
-    p.interval = interval;
-    p.n_rec = n_rec;
-    p.j0 = j0;
-    p.ntiles = coop_tiles(e, &p.tiles_x, &p.tiles_z);
-    p.plane = e->plane;
-    p.dt2_inj = dt2inj_f;
-    p.done = e->coop_done.p;
-    p.err = e->err.p;
-    return p;
-}
-
-cudaError_t launch_coop(w2d_engine* e, const AcPlan& p, const AcGeom& g)
-{
-    const int sp = sponge_mode(e);
-    if (e->tile.warps == 8) {
-        if (sp == SPONGE_LUT) return launch_acoustic_coop<8, 4, SPONGE_LUT>(p, g, e->stream);
-        if (sp == SPONGE_ARRAY) return launch_acoustic_coop<8, 4, SPONGE_ARRAY>(p, g, e->stream);
-        return launch_acoustic_coop<8, 4, SPONGE_NONE>(p, g, e->stream);
-    }
-    if (sp == SPONGE_LUT) return launch_acoustic_coop<4, 4, SPONGE_LUT>(p, g, e->stream);
-    if (sp == SPONGE_ARRAY) return launch_acoustic_coop<4, 4, SPONGE_ARRAY>(p, g, e->stream);
-    return launch_acoustic_coop<4, 4, SPONGE_NONE>(p, g, e->stream);
-}
-
 int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it1, double dt2inj,
                       float dt2inj_f)
 {
@@ -517,39 +436,6 @@ int run_forward_steps(w2d_engine* e, int slot, const FwdOpts& o, int it0, int it
             if (o.illum) s.illum = e->illum.p;
         }
     };
-    if (coop_mode(e) && it0 < it1) {
-        // cooperative launches of up to COOP_CHUNK steps, cut at the checkpoints
-        int rc;
-        if ((rc = coop_begin(e))) return rc;
-        unsigned j0 = 0;
-        for (int it = it0; it < it1;) {
-            if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
-                float* c = o.ckpt + (size_t)(it / o.ckpt_every) * 3 * e->plane;
-                W2D_CUDA_TRY(cudaMemcpyAsync(c, e->wave(it % 3), e->plane * 4,
-                                             cudaMemcpyDeviceToDevice, e->stream));
-                W2D_CUDA_TRY(cudaMemcpyAsync(c + e->plane, e->wave((it + 1) % 3), e->plane * 4,
-                                             cudaMemcpyDeviceToDevice, e->stream));
-                W2D_CUDA_TRY(cudaMemcpyAsync(c + 2 * e->plane, e->wave((it + 2) % 3),
-                                             e->plane * 4, cudaMemcpyDeviceToDevice, e->stream));
-            }
-            int end = std::min(it1, it + COOP_CHUNK);
-            if (o.ckpt && o.ckpt_every > 0)
-                end = std::min(end, (it / o.ckpt_every + 1) * o.ckpt_every);
-            AcPlan p = coop_plan(e, +1, it, end - it, o.nt, o.interval, o.n_rec, j0, slot,
-                                 dt2inj_f);
-            p.wavelet = e->cur_w;
-            p.rec_out = o.rec_out;
-            p.snaps = o.snaps;
-            p.slot0 = o.slot0;
-            p.illum = o.illum ? e->illum.p : nullptr;
-            W2D_CUDA_TRY(launch_coop(e, p, g));
-            e->last_launches++;
-            j0 += (unsigned)(end - it);
-            it = end;
-        }
-        (void)dt2inj;
-        return W2D_OK;
-    }
     for (int it = it0; it < it1;) {
         if (o.ckpt && o.ckpt_every > 0 && it % o.ckpt_every == 0) {
             e->chain = false;
@@ -618,26 +504,6 @@ int run_backward_steps(w2d_engine* e, int slot, int nt, int interval, int n_rec,
             }
         }
     };
-    if (coop_mode(e) && it_hi >= it_lo) {
-        int rc;
-        if ((rc = coop_begin(e))) return rc;
-        unsigned j0 = 0;
-        for (int it = it_hi; it >= it_lo;) {
-            const int S = std::min(COOP_CHUNK, it - it_lo + 1);
-            AcPlan p = coop_plan(e, -1, it, S, nt, interval, n_rec, j0, slot, dt2inj_f);
-            p.data = n_rec > 0 ? e->cur_data : nullptr;
-            p.snap_in = snaps;
-            p.slot0 = slot0;
-            p.n_snaps_valid = n_snaps_valid;
-            p.image = e->image.p;
-            p.img_dt = img_dt;
-            W2D_CUDA_TRY(launch_coop(e, p, g));
-            e->last_launches++;
-            j0 += (unsigned)S;
-            it -= S;
-        }
-        return W2D_OK;
-    }
     for (int it = it_hi; it >= it_lo;) {
         const int m = nt - 1 - it;
         int rc;
@@ -835,7 +701,6 @@ void w2d_engine_destroy(w2d_engine* e)
     e->err.release();
     e->scratch.release();
     e->tile_counter.release();
-    e->coop_done.release();
     for (auto& b : e->st_w) b.release();
     for (auto& b : e->st_d) b.release();
     if (e->t0) cudaEventDestroy(e->t0);
@@ -867,9 +732,8 @@ int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl)
 {
     W2D_ON_DEVICE_OF(e);
     W2D_CHECK_ARG(e, "engine is NULL");
-    W2D_CHECK_ARG(persistent >= 0 && persistent <= 2, "launch mode must be 0, 1 or 2");
     W2D_CUDA_TRY(cudaStreamSynchronize(e->stream));
-    e->persistent = persistent;
+    e->persistent = persistent ? 1 : 0;
     e->pdl = pdl ? 1 : 0;
     return W2D_OK;
 }

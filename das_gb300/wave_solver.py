@@ -115,21 +115,15 @@ class WaveSolver2D:
         if self._engine is not None:
             _lib.check(self._lib.w2d_engine_set_graphs(self._engine, 1 if on else 0))
 
-    _LAUNCH_KINDS = {"grid": 0, "persistent": 1, "coop": 2}
-
     def _apply_launch(self, h):
         kind, pdl = self.launch
-        if kind not in self._LAUNCH_KINDS:
-            raise ValueError(f"launch kind must be one of {sorted(self._LAUNCH_KINDS)}")
-        _lib.check(self._lib.w2d_engine_set_launch(h, self._LAUNCH_KINDS[kind], 1 if pdl else 0))
+        if kind not in ("grid", "persistent"):
+            raise ValueError("launch kind must be 'grid' or 'persistent'")
+        _lib.check(self._lib.w2d_engine_set_launch(h, 1 if kind == "persistent" else 0,
+                                                   1 if pdl else 0))
 
     def set_launch(self, kind: str = "grid", pdl: bool = True) -> None:
-        """Choose how the step kernels launch (results are identical in every mode):
-        "grid" one launch per step, one CTA per tile; "persistent" one launch per step,
-        resident CTAs drawing tiles from a counter; "coop" one cooperative launch per
-        run of up to 2048 steps, resident CTAs each advancing a static share of the
-        tiles step after step as soon as the neighbouring tiles are done (pdl applies
-        to the one-launch-per-step modes)."""
+        """Choose how the step kernels launch (results are identical in every mode)."""
         self.launch = (kind, bool(pdl))
         if self._engine is not None:
             self._apply_launch(self._engine)

@@ -104,14 +104,9 @@ int w2d_engine_set_tile(w2d_engine* e, int warps, int rows_per_warp);
 int w2d_engine_set_l2_hints(w2d_engine* e, int on);
 /* Step launch mode (results are bit-identical in every mode): persistent = 0 one
  * CTA per tile, 1 CTAs resident for the whole step taking tiles from a counter
- * with the next tile's boxes loading while the current one is computed, 2 one
- * cooperative launch per run of up to 2048 steps in which each resident CTA
- * advances a static share of the tiles, a tile starting step k as soon as its
- * 3 x 3 neighbour tiles have finished step k - 1 (no launch or grid barrier
- * between steps; 128 x 16 and 128 x 32 tiles, other shapes launch per step);
- * pdl = 1 launches each step as a programmatic dependent of the previous one, so
- * its set-up overlaps the previous step's tail (modes 0 and 1).  Default:
- * persistent 0, pdl 1. */
+ * with the next tile's boxes loading while the current one is computed; pdl = 1
+ * launches each step as a programmatic dependent of the previous one, so its
+ * set-up overlaps the previous step's tail.  Default: persistent 0, pdl 1. */
 int w2d_engine_set_launch(w2d_engine* e, int persistent, int pdl);
 /* CUDA graphs for migrations (on = 1, the default): the forward pass and the backward
  * pass of w2d_migrate_shot / w2d_migrate_staged are each captured once as a graph and

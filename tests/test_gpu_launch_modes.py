@@ -1,7 +1,5 @@
 """Step launch modes: one CTA per tile or persistent CTAs over a tile counter, each
-with or without programmatic dependent launch, and the time-persistent cooperative
-form (resident CTAs advancing their tiles step after step behind per-tile neighbour
-counters), give bit-identical results.
+with or without programmatic dependent launch, give bit-identical results.
 
 The persistent form draws tiles from a counter that is never reset between
 launches (each launch draws exactly ntiles + grid indices); long runs with
@@ -15,7 +13,7 @@ from oracle import oracle as o
 
 pytestmark = pytest.mark.gpu
 
-MODES = [("grid", False), ("persistent", False), ("persistent", True), ("coop", False)]
+MODES = [("grid", False), ("persistent", False), ("persistent", True)]
 
 
 def _solver(grid, tile, mode):
@@ -154,47 +152,3 @@ def test_graph_replays_equal_direct_launches(storage):
         np.testing.assert_array_equal(a[1], b[1], err_msg=f"illumination, shot {k}")
         assert a[2:] == b[2:] and a[4] == storage, (k, a[2:], b[2:])
         assert np.abs(a[0]).max() > 0
-
-
-@pytest.mark.parametrize("fs,custom_sponge,tile", [(True, False, (4, 4)), (False, True, (4, 4)),
-                                                   (True, True, (8, 4))])
-def test_coop_equals_grid_launch(fs, custom_sponge, tile):
-    """The time-persistent cooperative form against one launch per step: traces,
-    snapshots, backward image and both storage modes of migrate_shot bit-identical,
-    over 2301 steps (two cooperative launches per pass, the second of 253 steps),
-    with receivers on the never-written edge columns and repeated, the source in the
-    sponge frame, with and without free surface, and a caller-made sponge array (read
-    per cell)."""
-    from das_gb300.rtm_engine import TSWRTMEngine
-    from das_gb300.velocity_flood import FloodModels
-    from das_gb300.wave_solver import WaveSolver2D
-    nz, nx = 90, 420
-    rng = np.random.default_rng(23)
-    grid = o.Grid(nx, nz, 5.0, 5.0, 5e-4, 16, 0.003, fs)
-    v = rng.uniform(1500, 3200, (nz, nx)).astype(np.float32)
-    w, _ = o.ricker_wavelet(20.0, grid.dt, 1.1505)
-    assert len(w) == 2301
-    rix = np.concatenate([[0, 1, 1], np.sort(rng.integers(2, nx - 2, size=80)), [nx - 2, nx - 1]])
-    data = (rng.standard_normal((len(w), len(rix))) * 1e-6).astype(np.float32)
-    fm = FloodModels(v, v, (v * 1.01).astype(np.float32), 0, 0)
-    sponge = None
-    out = {}
-    for kind in ("coop", "grid"):
-        s = WaveSolver2D(nx, nz, grid.dx, grid.dz, grid.dt, grid.n_sponge, grid.sponge_alpha, fs)
-        s.tile = tile
-        if custom_sponge:
-            if sponge is None:
-                sponge = (s.sponge * rng.uniform(0.9, 1.0, s.sponge.shape)).astype(np.float32)
-            s.sponge = sponge
-        s.set_launch(kind, kind == "grid")
-        rec, snaps = s.forward_propagate_acoustic(v, w, 5, 2 if fs else 3, rix, 2, True, 2)
-        img = np.zeros((nz, nx), np.float32)
-        s.backward_propagate_and_correlate(v, data, rix, 2, snaps, img, 2)
-        res = [rec, snaps, img]
-        for storage in ("all", "checkpoint"):
-            res += list(TSWRTMEngine(s, storage).migrate_shot(fm, w, 8, 2, data, rix, 2, 2))
-        out[kind] = res
-        s.close()
-    for k, (a, b) in enumerate(zip(out["coop"], out["grid"])):
-        np.testing.assert_array_equal(a, b, err_msg=f"result {k}")
-    assert np.abs(out["coop"][2]).max() > 0
