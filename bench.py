@@ -352,6 +352,8 @@ def run_ours(args, dist):
     solver.l2_hints = bool(args.l2_hints)
     solver.set_launch(args.launch, bool(args.pdl))
     solver.set_graphs(bool(args.graphs))
+    if args.two_step:
+        solver.set_two_step(int(args.two_step))
     eng = solver._eng()
     K, W = args.steps, args.warmup
     n_sh = K + W
@@ -459,7 +461,7 @@ def run_ours(args, dist):
                           "shots_per_step": 1, "snapshot_interval": interval,
                           "storage": used, "tile": list(solver.tile or (4, 4)),
                           "launch": args.launch, "pdl": bool(args.pdl),
-                          "graphs": bool(args.graphs),
+                          "graphs": bool(args.graphs), "two_step": args.two_step,
                           "l2": L2_NOTE, "parallelism": f"shots sharded over {dist.world} GPU(s)"},
                "shots_per_s": K * dist.world / dev_s,
                "recomputed_steps_per_shot": recompute / max(K, 1),
@@ -965,6 +967,7 @@ def main():
     ap.add_argument("--launch", default="grid", choices=["grid", "persistent"])
     ap.add_argument("--pdl", type=int, default=1)
     ap.add_argument("--graphs", type=int, default=1)
+    ap.add_argument("--two-step", type=int, default=0)  # rows per warp of the two-step kernel
     ap.add_argument("--serve-jobs", type=int, default=40)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-side-scale", type=float, default=1.0)
