@@ -163,6 +163,9 @@ struct w2d_engine {
     // (which does not read it); the backward pass waits for data_ready
     cudaStream_t up = nullptr;
     cudaEvent_t up_after = nullptr, data_ready = nullptr;
+    // end of a migration's forward pass: its illumination is final and downloads on the
+    // upload stream while the backward pass runs
+    cudaEvent_t fwd_done = nullptr;
     bool data_pending = false;
 
     // stats of the last call
@@ -606,7 +609,8 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
         cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess ||
         cudaStreamCreateWithFlags(&e->up, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&e->up_after, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&e->data_ready, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&e->data_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fwd_done, cudaEventDisableTiming) != cudaSuccess) {
         set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
     }
@@ -710,6 +714,7 @@ void w2d_engine_destroy(w2d_engine* e)
     if (e->up) cudaStreamSynchronize(e->up);
     if (e->up_after) cudaEventDestroy(e->up_after);
     if (e->data_ready) cudaEventDestroy(e->data_ready);
+    if (e->fwd_done) cudaEventDestroy(e->fwd_done);
     if (e->up) cudaStreamDestroy(e->up);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -1040,6 +1045,7 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
     };
     if ((rc = run_pass(e, e->g_fwd, pass_key(e, 0, nt, interval, mode, seg, n_rec), forward)))
         return rc;
+    if (image_out) W2D_CUDA_TRY(cudaEventRecord(e->fwd_done, e->stream));
 
     // 2. backward pass in slot 1 with imaging
     if (e->data_pending) {  // the receiver data uploaded beside the forward pass
@@ -1084,9 +1090,17 @@ int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int st
         return rc;
     cudaEventRecord(e->ev1, e->stream);
     if (image_out) {
-        if ((rc = download_field(e, image_out, e->image.p)) ||
-            (rc = download_field(e, illum_out, e->illum.p)))
-            return rc;
+        // the illumination (final since the forward pass) comes back on the upload stream
+        // beside the backward pass; the image after it
+        cudaError_t ce = cudaStreamWaitEvent(e->up, e->fwd_done, 0);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy2DAsync(illum_out, (size_t)e->nx * 4, e->illum.p, (size_t)e->ldx * 4,
+                                   (size_t)e->nx * 4, e->nz, cudaMemcpyDeviceToHost, e->up);
+        const int rc_img = download_field(e, image_out, e->image.p);
+        const cudaError_t se = cudaStreamSynchronize(e->up);
+        W2D_CUDA_TRY(ce);
+        if (rc_img) return rc_img;
+        W2D_CUDA_TRY(se);
     } else {
         if ((rc = e->stack_img.ensure(e->plane)) || (rc = e->stack_ill.ensure(e->plane))) return rc;
         add_kernel<<<grid_for(e->plane), 256, 0, e->stream>>>(e->stack_img.p, e->image.p, e->plane);
