@@ -988,7 +988,7 @@ def main():
     ap.add_argument("--storage", default="auto", choices=["auto", "all", "checkpoint"])
     ap.add_argument("--tile", default="")
     ap.add_argument("--cpu-nt", type=int, default=1500)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--accuracy", type=int, default=1)
     ap.add_argument("--distinct-gathers", type=int, default=2)
     args = ap.parse_args()

@@ -46,7 +46,6 @@ constexpr int XC_TP = 4;        // warps sharing one lag group, each over a quar
 constexpr int XC_LAGS = XC_LG * (XC_WY / XC_TP);  // lags per CTA
 constexpr int XC_CHUNK = 1024;  // source samples staged per shared-memory chunk
 constexpr int XC_PART = XC_CHUNK / XC_TP;  // samples of a chunk per warp
-constexpr int XC_BATCH = 8;  // windows correlated per launch (their CTAs make many waves)
 static_assert(XC_WY % XC_TP == 0 && XC_PART % XC_LG == 0,
               "every warp's part of a chunk holds whole rounds of the register ring");
 
@@ -71,28 +70,18 @@ __global__ void xc_gather_kernel(const float* __restrict__ data, int nt, int n_c
     }
 }
 
-// Sample counts of the windows of one launch.
-struct XcWindows {
-    int nt[XC_BATCH];
-};
-
-// out[w][s][row][r] = float32(sum_t S_w[s][t] * R_w[t + lag0 + row][r]) for the windows w
-// of one launch (blockIdx.z = w * n_src + s); window w's traces at S + w s_stride and
-// Rp + w r_stride, its correlations at out + w out_stride.
+// stack[s][row][r] (+)= float32(sum_t S[s][t] * R[t + lag0 + row][r])
 __global__ void __launch_bounds__(XC_RX * XC_WY)
-    xc_kernel(const float* __restrict__ S, size_t s_stride, const float* __restrict__ Rp,
-              size_t r_stride, XcWindows win, int n_src, int n_rec, int pad, int lag0,
-              int n_rows, float* __restrict__ out, size_t out_stride)
+    xc_kernel(const float* __restrict__ S, const float* __restrict__ Rp, int nt, int n_rec,
+              int pad, int lag0, int n_rows, float* __restrict__ stack, int first)
 {
     __shared__ float s_src[XC_CHUNK];
     __shared__ float s_part[XC_WY][2][XC_LG][XC_RX];  // the parts' (hi, lo) sums
     const int r = blockIdx.x * XC_RX + threadIdx.x;
     const int grp = threadIdx.y % (XC_WY / XC_TP), part = threadIdx.y / (XC_WY / XC_TP);
     const int row0 = blockIdx.y * XC_LAGS + grp * XC_LG;
-    const int wi = blockIdx.z / n_src, s = blockIdx.z - wi * n_src;
-    const int nt = win.nt[wi];
-    Rp += wi * r_stride;
-    const float* Ss = S + wi * s_stride + (size_t)s * nt;
+    const int s = blockIdx.z;
+    const float* Ss = S + (size_t)s * nt;
     const int rr = min(r, n_rec - 1);  // lanes past the last receiver compute a copy
     // row of Rp holding R[t + lag0 + row0] at t = 0
     const long long base = (long long)pad + lag0 + row0;
@@ -170,20 +159,9 @@ __global__ void __launch_bounds__(XC_RX * XC_WY)
         }
         const int row = row0 + j;
         if (row >= n_rows) break;
-        out[wi * out_stride + ((size_t)s * n_rows + row) * n_rec + r] = __fadd_rn(h, l);
-    }
-}
-
-// The windows' correlations added to the float32 stack in window order, as one window at
-// a time would add them: the first window ever is copied, every later one added.
-__global__ void xc_stack_kernel(const float* __restrict__ corr, int n_win, size_t n,
-                                float* __restrict__ stack, int first)
-{
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x) {
-        float v = first ? corr[i] : __fadd_rn(stack[i], corr[i]);
-        for (int w = 1; w < n_win; ++w) v = __fadd_rn(v, corr[w * n + i]);
-        stack[i] = v;
+        float* o = stack + ((size_t)s * n_rows + row) * n_rec + r;
+        const float c = __fadd_rn(h, l);
+        *o = first ? c : __fadd_rn(*o, c);
     }
 }
 
@@ -357,49 +335,18 @@ struct w2d_xcorr {
     int nt = 0, n_ch = 0, n_src = 0, n_rec = 0, lag0 = 0, n_rows = 0, pad = 0, n_added = 0;
     int n_lags = 0;
     size_t r_rows = 0;  // rows of the zero-padded receiver buffer
+    int last_nt = 0;    // samples of the previous window (its rows must be cleared)
     int* d_src = nullptr;
     int* d_rec = nullptr;
     float* d_data[2] = {nullptr, nullptr};  // host windows land here, alternately
     cudaEvent_t gathered[2] = {nullptr, nullptr};  // the gather that read d_data[i] is done
     cudaStream_t st_copy = nullptr;
-    // windows waiting for one correlation launch (up to XC_BATCH), each in its own slot
-    int pending = 0, n_stacked = 0;
-    int slot_nt[XC_BATCH] = {0};
-    int slot_last_nt[XC_BATCH] = {0};  // samples of the slot's previous window
-    float* d_s = nullptr;     // per slot (n_src, nt)
-    float* d_r = nullptr;     // per slot (r_rows, n_rec), zero-padded
-    float* d_corr = nullptr;  // per slot (n_src, n_rows, n_rec): that window's correlations
+    float* d_s = nullptr;     // (n_src, nt)
+    float* d_r = nullptr;     // (nt + 2*pad, n_rec), zero-padded
     float* d_stack = nullptr; // (n_src, n_rows, n_rec)
     float* d_out = nullptr;   // read-back staging
     cudaStream_t st = nullptr;
 };
-
-namespace {
-
-// Correlate the queued windows in one launch (XC_BATCH windows make many waves of CTAs
-// where one window makes under two), each into its own slot, then add them to the stack
-// in window order.
-int xc_flush(w2d_xcorr* x)
-{
-    if (x->pending == 0) return W2D_OK;
-    XcWindows win;
-    for (int k = 0; k < XC_BATCH; ++k) win.nt[k] = x->slot_nt[k];
-    const size_t corr_n = (size_t)x->n_src * x->n_rows * x->n_rec;
-    dim3 grid((x->n_rec + XC_RX - 1) / XC_RX, (x->n_rows + XC_LAGS - 1) / XC_LAGS,
-              x->n_src * x->pending);
-    xc_kernel<<<grid, dim3(XC_RX, XC_WY), 0, x->st>>>(
-        x->d_s, (size_t)x->n_src * x->nt, x->d_r, x->r_rows * x->n_rec, win, x->n_src,
-        x->n_rec, x->pad, x->lag0, x->n_rows, x->d_corr, corr_n);
-    W2D_CUDA_TRY(cudaGetLastError());
-    xc_stack_kernel<<<grid_1d(corr_n), 256, 0, x->st>>>(x->d_corr, x->pending, corr_n,
-                                                        x->d_stack, x->n_stacked == 0 ? 1 : 0);
-    W2D_CUDA_TRY(cudaGetLastError());
-    x->n_stacked += x->pending;
-    x->pending = 0;
-    return W2D_OK;
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -455,20 +402,19 @@ int w2d_xcorr_create(w2d_xcorr** out, int nt, int n_ch, const int* src_ch, int n
         set_error("stream/event creation failed");
         return fail(W2D_ECUDA);
     }
-    size_t c0 = 0, c1 = 0, c2 = 0, c2b = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0, c7 = 0;
-    const size_t corr_n = (size_t)n_src * std::max(1, x->n_rows) * n_rec;
+    size_t c0 = 0, c1 = 0, c2 = 0, c2b = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0;
     int rc;
     if ((rc = grow(&x->d_src, &c0, n_src)) || (rc = grow(&x->d_rec, &c1, n_rec)) ||
         (rc = grow(&x->d_data[0], &c2, (size_t)nt * n_ch)) ||
         (rc = grow(&x->d_data[1], &c2b, (size_t)nt * n_ch)) ||
-        (rc = grow(&x->d_s, &c3, (size_t)XC_BATCH * n_src * nt)) ||
-        (rc = grow(&x->d_r, &c4, (size_t)XC_BATCH * r_rows * n_rec)) ||
-        (rc = grow(&x->d_corr, &c7, (size_t)XC_BATCH * corr_n)) ||
-        (rc = grow(&x->d_stack, &c5, corr_n)) || (rc = grow(&x->d_out, &c6, corr_n)))
+        (rc = grow(&x->d_s, &c3, (size_t)n_src * nt)) ||
+        (rc = grow(&x->d_r, &c4, (size_t)r_rows * n_rec)) ||
+        (rc = grow(&x->d_stack, &c5, (size_t)n_src * std::max(1, x->n_rows) * n_rec)) ||
+        (rc = grow(&x->d_out, &c6, (size_t)n_src * std::max(1, x->n_rows) * n_rec)))
         return fail(rc);
     if (cudaMemcpy(x->d_src, src_ch, n_src * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(x->d_rec, rec_ch, n_rec * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(x->d_r, 0, (size_t)XC_BATCH * r_rows * n_rec * 4) != cudaSuccess ||
+        cudaMemset(x->d_r, 0, (size_t)r_rows * n_rec * 4) != cudaSuccess ||
         cudaMemset(x->d_stack, 0, (size_t)n_src * std::max(1, x->n_rows) * n_rec * 4) !=
             cudaSuccess) {
         set_error("cross-correlation set-up failed");
@@ -486,8 +432,7 @@ void w2d_xcorr_destroy(w2d_xcorr* x)
     if (x->st) cudaStreamSynchronize(x->st);
     if (x->st_copy) cudaStreamSynchronize(x->st_copy);
     for (void* p : {(void*)x->d_src, (void*)x->d_rec, (void*)x->d_data[0], (void*)x->d_data[1],
-                    (void*)x->d_s, (void*)x->d_r, (void*)x->d_corr, (void*)x->d_stack,
-                    (void*)x->d_out})
+                    (void*)x->d_s, (void*)x->d_r, (void*)x->d_stack, (void*)x->d_out})
         if (p) cudaFree(p);
     for (cudaEvent_t ev : x->gathered)
         if (ev) cudaEventDestroy(ev);
@@ -515,28 +460,23 @@ int w2d_xcorr_add_device(w2d_xcorr* x, const float* data_dev, int nt)
     // the reference's stack (ndarray +=) needs every window's correlation rows to agree
     W2D_CHECK_ARG(lag0 == x->lag0 && n_rows == x->n_rows,
                   "this window's correlation rows differ from the stack's");
-    W2D_CHECK_ARG((x->n_rows + XC_LAGS - 1) / XC_LAGS <= 65535 &&
-                      (long long)x->n_src * XC_BATCH <= 65535,
+    W2D_CHECK_ARG((x->n_rows + XC_LAGS - 1) / XC_LAGS <= 65535 && x->n_src <= 65535,
                   "too many lags or sources for one launch");
     if (x->n_rows > 0) {
-        // this window's traces into the next free slot; the correlation runs when the
-        // slots are full or the stack is read
-        const int k = x->pending;
-        float* ds = x->d_s + (size_t)k * x->n_src * x->nt;
-        float* dr = x->d_r + (size_t)k * x->r_rows * x->n_rec;
-        if (x->slot_last_nt[k] > nt)  // rows of a longer earlier window must read as zero
-            W2D_CUDA_TRY(cudaMemsetAsync(dr + (size_t)(x->pad + nt) * x->n_rec, 0,
-                                         (size_t)(x->slot_last_nt[k] - nt) * x->n_rec * 4,
-                                         x->st));
+        if (x->last_nt > nt)  // rows of a longer previous window must read as zero again
+            W2D_CUDA_TRY(cudaMemsetAsync(x->d_r + (size_t)(x->pad + nt) * x->n_rec, 0,
+                                         (size_t)(x->last_nt - nt) * x->n_rec * 4, x->st));
         xc_gather_kernel<<<grid_1d((size_t)nt * (x->n_rec + x->n_src)), 256, 0, x->st>>>(
-            data_dev, nt, x->n_ch, x->d_src, x->n_src, x->d_rec, x->n_rec, x->pad, ds, dr);
+            data_dev, nt, x->n_ch, x->d_src, x->n_src, x->d_rec, x->n_rec, x->pad, x->d_s,
+            x->d_r);
+        dim3 grid((x->n_rec + XC_RX - 1) / XC_RX, (x->n_rows + XC_LAGS - 1) / XC_LAGS, x->n_src);
+        xc_kernel<<<grid, dim3(XC_RX, XC_WY), 0, x->st>>>(x->d_s, x->d_r, nt, x->n_rec, x->pad,
+                                                          x->lag0, x->n_rows, x->d_stack,
+                                                          x->n_added == 0 ? 1 : 0);
         W2D_CUDA_TRY(cudaGetLastError());
-        x->slot_nt[k] = nt;
-        x->slot_last_nt[k] = nt;
-        x->pending++;
     }
+    x->last_nt = nt;
     x->n_added++;
-    if (x->pending == XC_BATCH) return xc_flush(x);
     return W2D_OK;
 }
 
@@ -564,8 +504,6 @@ int w2d_xcorr_read(w2d_xcorr* x, float* out_host, int divide)
     W2D_ON_DEVICE_OF(x);
     W2D_CHECK_ARG(x && out_host, "NULL argument");
     W2D_CHECK_ARG(x->n_added > 0, "no window added");
-    int rc;
-    if ((rc = xc_flush(x))) return rc;
     const size_t n = (size_t)x->n_src * x->n_rows * x->n_rec;
     if (n) {
         const float* src = x->d_stack;

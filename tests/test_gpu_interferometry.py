@@ -80,51 +80,6 @@ def test_stack_from_device_windows_equals_host_windows(golden):
         np.testing.assert_array_equal(ra[s][0], rb[s][0])
 
 
-def test_stack_across_correlation_batches(golden):
-    """A stack correlates queued windows several at a time (one launch per batch, each
-    window into its own buffer, then added to the stack in window order).  Nineteen
-    windows of mixed lengths (more than two batches, with a read in the middle, which
-    correlates a partial batch) must give, bit for bit, the float32 stack of the
-    windows' correlations taken one window at a time."""
-    from das_gb300.interferometry import CrossCorrelationStack
-    g = golden("interferometry")
-    dt = float(g["dt"])
-    n_ch = g["data0"].shape[1]
-    rng = np.random.default_rng(41)
-    base = np.concatenate([g["data0"], g["data1"], g["data2"]])
-    wins = []
-    for k in range(19):
-        n = int(rng.integers(1300, 1501))
-        o0 = int(rng.integers(0, base.shape[0] - n))
-        wins.append(np.ascontiguousarray(base[o0:o0 + n]))
-    singles = []
-    for w in wins:
-        one = CrossCorrelationStack(1500, n_ch, g["src"], g["rec"], 2.0, dt)
-        one.add(w)
-        singles.append(one.result(divide=False))
-        one.close()
-    st = CrossCorrelationStack(1500, n_ch, g["src"], g["rec"], 2.0, dt)
-    for k, w in enumerate(wins):
-        st.add(w)
-        if k == 10:
-            mid = st.result(divide=False)
-            for s in mid:
-                ref = singles[0][s][0].copy()
-                for j in range(1, 11):
-                    ref = (ref + singles[j][s][0]).astype(np.float32)
-                np.testing.assert_array_equal(mid[s][0], ref)
-    res = st.result(divide=False)
-    for s in res:
-        ref = singles[0][s][0].copy()
-        for j in range(1, len(wins)):
-            ref = (ref + singles[j][s][0]).astype(np.float32)
-        np.testing.assert_array_equal(res[s][0], ref)
-    avg = st.result()
-    for s in avg:
-        np.testing.assert_array_equal(avg[s][0], (res[s][0] / np.float32(len(wins))).astype(np.float32))
-    st.close()
-
-
 def test_derivatives_branches_resampling_golden(golden):
     from das_gb300.interferometry import (build_virtual_shot_gather, full_green_function,
                                           resample_gather_to_sim_dt, time_derivative_greens)
