@@ -64,6 +64,8 @@ struct AcStep {
     const float* inj_data;   // backward: receiver-data row of the next step
     float dt2_inj;           // float32(dt**2) as the Python drivers compute it
     unsigned* err;
+    int early;               // p_prev and the model may be read before the dependency
+                             // wait (acoustic_step_kernel): nothing still running writes them
 };
 
 // The TMA descriptors of one tile-step.
@@ -134,6 +136,36 @@ __device__ __forceinline__ void ac_issue_loads(float* smem, const AcMaps* m, int
     }
     if (SPONGE == SPONGE_ARRAY)
         tma_load_2d(smem + T::C_FLOATS + 2 * T::P_FLOATS, &m->sponge, x0, z0, bar);
+}
+
+// The boxes of a tile that only earlier steps wrote (p_prev, v^2 dt^2, the sponge
+// array), expecting the whole tile's bytes on `bar`; then the p_curr box with its halo.
+template <int WARPS, int RPW, int SPONGE>
+__device__ __forceinline__ void ac_issue_own(float* smem, const AcMaps* m, int x0, int z0,
+                                             uint64_t* bar, int l2_hints)
+{
+    using T = AcTile<WARPS, RPW, SPONGE>;
+    mbar_expect_tx(bar, T::TX_BYTES);
+    if (l2_hints) {
+        tma_load_2d_hint(smem + T::C_FLOATS, &m->prev, x0, z0, bar, policy_evict_first());
+        tma_load_2d_hint(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar,
+                         policy_evict_last());
+    } else {
+        tma_load_2d(smem + T::C_FLOATS, &m->prev, x0, z0, bar);
+        tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &m->vel, x0, z0, bar);
+    }
+    if (SPONGE == SPONGE_ARRAY)
+        tma_load_2d(smem + T::C_FLOATS + 2 * T::P_FLOATS, &m->sponge, x0, z0, bar);
+}
+
+template <int WARPS, int RPW, int SPONGE>
+__device__ __forceinline__ void ac_issue_curr(float* smem, const AcMaps* m, int x0, int z0,
+                                              uint64_t* bar, int l2_hints)
+{
+    if (l2_hints)
+        tma_load_2d_hint(smem, &m->curr, x0 - AC_HX, z0 - 2, bar, policy_evict_last());
+    else
+        tma_load_2d(smem, &m->curr, x0 - AC_HX, z0 - 2, bar);
 }
 
 // True when no cell of the tile needs boundary, sponge, source or receiver work.
@@ -388,20 +420,29 @@ __global__ void __launch_bounds__(WARPS * 32)
         prefetch_tensormap(&maps.curr);
         mbar_init(bar, 1);
         fence_mbar_init();
+        // Early: p_prev was written by the step before the previous one and the model
+        // long before.  Each step kernel triggers its dependents only after its own
+        // dependency wait (below), so this kernel started after that step had completed:
+        // these boxes go out while the previous step still drains.
+        if (s.early) ac_issue_own<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     }
-    // the set-up above overlaps the previous step's tail when launched as a
-    // programmatic dependent; nothing of the previous step is read before the wait
-    grid_dep_launch();
-    grid_dep_wait();
-    if (threadIdx.x == 0) ac_issue_loads<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     if (s.snap_in && threadIdx.x < T::TZ && z0 + (int)threadIdx.x < g.nz) {
-        // imaging steps read the forward snapshot from HBM after the stencil: start
-        // bringing the tile's rows into L2 now, beside the boxes (one row per thread,
+        // imaging steps read the forward snapshot (written in the forward pass) from HBM
+        // after the stencil: bring the tile's rows into L2 now (one row per thread,
         // within the row pitch).  (Prefetching the next imaging step's rows one step
         // ahead as well measured no better.)
         const int row = z0 + threadIdx.x;
         prefetch_l2_bulk(s.snap_in + (size_t)row * g.ldx + x0,
                          (uint32_t)min(AC_TX, g.ldx - x0) * 4u);
+    }
+    // p_curr is the previous step's output: read only after the wait.  The dependents
+    // are released after it, so the next step cannot start before this one's
+    // predecessor has completed (what makes the next step's early boxes safe).
+    grid_dep_wait();
+    grid_dep_launch();
+    if (threadIdx.x == 0) {
+        if (!s.early) ac_issue_own<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
+        ac_issue_curr<WARPS, RPW, SPONGE>(smem, &maps, x0, z0, bar, g.l2_hints);
     }
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined

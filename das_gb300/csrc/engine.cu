@@ -114,6 +114,7 @@ struct w2d_engine {
     int persistent = 0, pdl = 1;  // step launch mode (measured fastest: one CTA per tile + PDL)
     int fwi_seg = 0;  // differentiable path: steps per checkpoint segment (0: sqrt(3 nt))
     bool chain = false;  // the last operation on the stream is a step kernel launched by step()
+    bool last_step1 = false;  // ... and it was the one-step kernel (one CTA per tile)
     DevBuf<unsigned> tile_counter;
     unsigned counter_base = 0;
 
@@ -307,9 +308,15 @@ int step(w2d_engine* e, int curr, int prev, int slot, const AcGeom& g, const AcS
     lm.pdl = e->pdl && e->chain;
     lm.counter = e->tile_counter.p;
     lm.base = &e->counter_base;
+    // early reads of p_prev and the model: safe after a one-step kernel of the chain
+    // (it releases this launch only after its own wait) or without a dependency at all;
+    // not after a two-step launch, which wrote p_prev itself
+    AcStep se = s;
+    se.early = (!lm.pdl || e->last_step1) ? 1 : 0;
     e->chain = false;
-    W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), lm, m, g, s, e->stream));
+    W2D_CUDA_TRY(launch_step(e->tile, sponge_mode(e), lm, m, g, se, e->stream));
     e->chain = true;
+    e->last_step1 = !e->persistent;
     e->last_launches++;
     return W2D_OK;
 }
@@ -337,6 +344,7 @@ int step2(w2d_engine* e, int pass, int curr, int prev, int next, int slot, const
     e->chain = false;
     W2D_CUDA_TRY(launch_acoustic_step2(e->two_step, sponge_mode(e), m, g, p, e->stream, pdl));
     e->chain = true;
+    e->last_step1 = false;  // it wrote the next step's p_prev itself
     e->last_launches++;
     const int old_next = e->perm[next], old_prev = e->perm[prev];
     e->perm[next] = sp[0];
