@@ -238,10 +238,10 @@ __global__ void __launch_bounds__(WARPS * 32, RPW <= 4 ? 1024 / (WARPS * 32) : 1
         mbar_init(bar, 1);
         fence_mbar_init();
     }
-    grid_dep_launch();
-    // The work table and the shots' fixed fields do not change during a replay (they are
-    // written before its first launch, which waits for the stream normally): read them
-    // while the previous launch drains.  The progress k0 changes between chunks.
+    // The work table and the shots' descriptors do not change during a replay (they are
+    // written before its first launch, which waits for the stream normally; the progress
+    // k0 moves only in the progress kernel that ends a replay): read them while the
+    // previous launch drains.
     const int2 it = __ldg(a.items + blockIdx.x);
     const int slot = it.x, t = it.y;
     if (slot < 0 || slot >= a.max_shots || t < 0) {  // inconsistent work table: skip, report
@@ -251,20 +251,25 @@ __global__ void __launch_bounds__(WARPS * 32, RPW <= 4 ? 1024 / (WARPS * 32) : 1
     }
     const BShot* sh = a.shots + slot;
     const int ntiles = sh->ntiles, k_end = sh->k_end;
-    grid_dep_wait();
     const int k = sh->k0 + a.j;
-    if (t >= ntiles || k >= k_end) return;
+    if (t >= ntiles || k >= k_end) return;  // an exited CTA counts as released
     AcStep s;
     int ci, pi, vi;
     batch_phase(sh, k, a.err, s, ci, pi, vi);
     const BMaps* mp = a.maps + sh->maps_index;
     const int x0 = (t % sh->tiles_x) * AC_TX, z0 = (t / sh->tiles_x) * T::TZ;
     if (tid == 0) {
+        // p_prev is the output of the launch before the previous one (or older), the model
+        // older still.  Every launch releases its dependents only after its own wait, so
+        // this one started after that launch had completed: these boxes go out now.
         mbar_expect_tx(bar, T::TX_BYTES);
-        tma_load_2d(smem, &mp->curr[ci], x0 - AC_HX, z0 - 2, bar);
         tma_load_2d(smem + T::C_FLOATS, &mp->prev[pi], x0, z0, bar);
         tma_load_2d(smem + T::C_FLOATS + T::P_FLOATS, &mp->vel[vi], x0, z0, bar);
     }
+    // p_curr is the previous launch's output: after the wait
+    grid_dep_wait();
+    grid_dep_launch();
+    if (tid == 0) tma_load_2d(smem, &mp->curr[ci], x0 - AC_HX, z0 - 2, bar);
     if ((s.snap_in || s.image || s.illum) && tid < 3 * T::TZ) {
         // the fused pointwise work reads these planes from HBM after the stencil (a
         // batch's planes do not stay in L2): bring the tile's rows into L2 beside the
