@@ -75,6 +75,7 @@ struct w2d_elastic {
     // is a kernel of the step / tiled-adjoint chain (a launch may depend on it only then)
     int pdl = 1;
     bool chain = false;
+    bool last_stress = false;  // ... and that kernel was a stress phase
     CUtensorMap adj_map_tmp;                // the adjoint passes' maps (their own box height)
     std::vector<CUtensorMap> adj_seg_maps;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -160,9 +161,14 @@ int fwd_step(w2d_elastic* e, const CUtensorMap& msrc, const CUtensorMap& mdst, c
         st.rec_iz = e->rec_iz;
         st.trace_stride = (size_t)e->nt * e->n_rec;
     }
+    // the velocity phase stages its fields early after a stress phase of the chain (it
+    // releases its dependents only after its own wait) or with no dependency at all
+    const int pdl = e->pdl && e->chain;
+    st.early = (!pdl || e->last_stress) ? 1 : 0;
     W2D_CUDA_TRY(launch_elastic_step(egeom(e), m, st, e->st, e->S, e->map_fwd_warps,
-                                     e->map_fwd_rpw, e->pdl && e->chain));
+                                     e->map_fwd_rpw, pdl));
     e->chain = true;
+    e->last_stress = true;
     return W2D_OK;
 }
 
@@ -459,6 +465,7 @@ int w2d_elastic_gradient_batch(w2d_elastic* e, const float* resid_dev, float* g_
                 W2D_CUDA_TRY(launch_el_adj_b(m, g, prm, sd, a, t, n >= 1 ? 1 : 0, e->err, S,
                                              e->st, e->map_adj_warps, e->map_adj_rpw, e->pdl));
                 e->chain = true;
+                e->last_stress = false;
             } else {
                 e->chain = false;
                 ElState f_next = e->S0(e->slot(n + 1 - a0));  // u_{n+1}

@@ -66,6 +66,9 @@ struct ElStep {
     const int* rec_list = nullptr;
     int rec_iz = 0;
     size_t trace_stride = 0;
+    // the pointwise fields may be staged before the dependency wait: the launch two back
+    // wrote them (or nothing running does), see the phases' kernels
+    int early = 0;
 };
 
 struct ElMaps {
@@ -209,16 +212,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         mbar_init(bar, 1);
         fence_mbar_init();
     }
-    // the set-up above overlaps the previous kernel's tail when launched as a
-    // programmatic dependent; every thread waits before any global access
-    grid_dep_launch();
-    grid_dep_wait();
-    if (tid == 0) {
-        mbar_expect_tx(bar, 3u * T::BOX * 4u);
-        tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXX, bar);
-        tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXZ, bar);
-        tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SZZ, bar);
-    }
     // every lane takes part in the shuffles; lanes past the row pitch only skip
     // their loads and stores
     const int ixb = x0 + 4 * lane;
@@ -232,10 +225,22 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* bxp = s.bx + po;
     const float* bzp = s.bz + po;
     const int zr0 = z0 + warp * RPW;
-    {
-        const float* f[5] = {vx_s, vz_s, bxp, bzp, g.sponge};
-        el_stage_pointwise<WARPS, RPW>(pt, f, 5, zr0, ixb, lane, warp, g);
+    const float* f[5] = {vx_s, vz_s, bxp, bzp, g.sponge};
+    // Early: the velocities were written by the velocity phase of the previous step
+    // (two launches back) and the buoyancies and sponge are constant.  Each phase
+    // releases its dependents only after its own wait, so this launch started after that
+    // one had completed, and the stress phase still running only reads velocities.
+    if (s.early) el_stage_pointwise<WARPS, RPW>(pt, f, 5, zr0, ixb, lane, warp, g);
+    // the stresses are the previous launch's output: after the wait
+    grid_dep_wait();
+    grid_dep_launch();
+    if (tid == 0) {
+        mbar_expect_tx(bar, 3u * T::BOX * 4u);
+        tma_load_3d(bxx, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXX, bar);
+        tma_load_3d(bxz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SXZ, bar);
+        tma_load_3d(bzz, &maps.src, x0 - EL_HX, z0 - 2, 5 * sh + EL_SZZ, bar);
     }
+    if (!s.early) el_stage_pointwise<WARPS, RPW>(pt, f, 5, zr0, ixb, lane, warp, g);
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
     if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
@@ -323,13 +328,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         mbar_init(bar, 1);
         fence_mbar_init();
     }
-    grid_dep_launch();
-    grid_dep_wait();  // as in the velocity phase
-    if (tid == 0) {
-        mbar_expect_tx(bar, 2u * T::BOX * 4u);
-        tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
-        tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
-    }
     const int ixb = x0 + 4 * lane;
     const bool col_ok = ixb < g.ldx;  // see the velocity phase
     const bool in_place = s.src == s.dst;
@@ -343,10 +341,20 @@ __global__ void __launch_bounds__(WARPS * 32)
     const float* lamp = s.lam + po;
     const float* mup = s.mu + po;
     const int zr0 = z0 + warp * RPW;
-    {
-        const float* f[6] = {lamp, mup, sxx_s, szz_s, sxz_s, g.sponge};
-        el_stage_pointwise<WARPS, RPW>(pt, f, 6, zr0, ixb, lane, warp, g);
+    const float* f[6] = {lamp, mup, sxx_s, szz_s, sxz_s, g.sponge};
+    // Early: the stresses were written by the stress phase of the previous step (two
+    // launches back), lambda, mu and the sponge are constant; the velocity phase still
+    // running only reads stresses.
+    if (s.early) el_stage_pointwise<WARPS, RPW>(pt, f, 6, zr0, ixb, lane, warp, g);
+    // the new velocities are the previous launch's output: after the wait
+    grid_dep_wait();
+    grid_dep_launch();
+    if (tid == 0) {
+        mbar_expect_tx(bar, 2u * T::BOX * 4u);
+        tma_load_3d(bvx, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VX, bar);
+        tma_load_3d(bvz, &maps.dst, x0 - EL_HX, z0 - 2, 5 * sh + EL_VZ, bar);
     }
+    if (!s.early) el_stage_pointwise<WARPS, RPW>(pt, f, 6, zr0, ixb, lane, warp, g);
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
     if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
@@ -515,6 +523,7 @@ cudaError_t launch_elastic_step_t(const ElGeom& g, const ElMaps& maps, const ElS
     if (e != cudaSuccess) return e;
     ElStep s2 = s;
     s2.src_pos = nullptr;
+    s2.early = 1;  // after the velocity kernel, which releases it only after its own wait
     // the stress phase always follows the velocity kernel directly
     return el_launch(elastic_stress_kernel<WARPS, RPW>, grid, dim3(WARPS * 32), sbytes, st, 1,
                      maps, g, s2);
