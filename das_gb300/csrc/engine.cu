@@ -193,7 +193,8 @@ struct w2d_engine {
             key.clear();
         }
     };
-    PassGraph g_fwd, g_bwd;
+    PassGraph g_fwd, g_bwd;    // a migration's two passes
+    PassGraph g_model, g_bcorr;  // forward modelling, backward propagation with imaging
     int use_graphs = 1;
 
     float* wave(int i) { return waves.p + (size_t)perm[i] * plane; }  // logical plane i
@@ -549,6 +550,69 @@ int backward_begin(w2d_engine* e, int nt, int n_rec, float dt2inj_f)
     return W2D_OK;
 }
 
+// Everything a pass's launches hold: when it matches a cached graph, replaying the
+// graph issues exactly the launches the host code would.
+std::vector<uintptr_t> pass_key(const w2d_engine* e, int pass, int nt, int interval, int mode,
+                                int seg, int n_rec)
+{
+    std::vector<uintptr_t> k = {
+        (uintptr_t)pass, (uintptr_t)nt, (uintptr_t)interval, (uintptr_t)mode, (uintptr_t)seg,
+        (uintptr_t)n_rec, (uintptr_t)e->tile.warps, (uintptr_t)e->tile.rpw, (uintptr_t)e->pdl,
+        (uintptr_t)e->l2_hints, (uintptr_t)e->use_lut, (uintptr_t)e->use_arr,
+        (uintptr_t)e->tm_tz, (uintptr_t)e->waves.p, (uintptr_t)e->snaps.p, (uintptr_t)e->ckpt.p,
+        (uintptr_t)e->v2dt2.p, (uintptr_t)e->image.p, (uintptr_t)e->illum.p,
+        (uintptr_t)e->cur_w, (uintptr_t)e->cur_data, (uintptr_t)e->rec_ptr.p,
+        (uintptr_t)e->rec_list.p, (uintptr_t)e->shot.p, (uintptr_t)e->err.p,
+        (uintptr_t)e->sponge_lut.p, (uintptr_t)e->sponge_arr.p, (uintptr_t)e->rec_out.p};
+    for (int i = 0; i < 6; ++i) k.push_back((uintptr_t)e->perm[i]);
+    return k;
+}
+
+// Run one pass: replay its cached graph when the key matches, else capture the pass
+// from `body` (the host code that launches it), instantiate and launch the graph.  With
+// graphs off, or in a launch mode that keeps host-side state, `body` runs directly.  A
+// capture the runtime refuses turns graphs off for this engine and runs `body`.
+template <typename F>
+int run_pass(w2d_engine* e, w2d_engine::PassGraph& pg, std::vector<uintptr_t> key, F&& body)
+{
+    if (!e->use_graphs || e->two_step || e->persistent) return body();
+    if (pg.exec && pg.key == key) {
+        W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
+        e->last_launches += pg.launches;
+        e->last_recompute += pg.recompute;
+        return W2D_OK;
+    }
+    pg.reset();
+    const long long l0 = e->last_launches, r0 = e->last_recompute;
+    W2D_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = body();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+    if (rc || ce != cudaSuccess || !graph) {
+        // Nothing captured has run.  Whatever refused the capture (the pass's own
+        // launches are checked again below), run this and later passes as direct
+        // launches on this engine.
+        cudaGetLastError();
+        if (graph) cudaGraphDestroy(graph);
+        e->use_graphs = 0;
+        e->last_launches = l0;
+        e->last_recompute = r0;
+        return body();
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&pg.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        pg.exec = nullptr;
+        set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+        return W2D_ECUDA;
+    }
+    pg.key = std::move(key);
+    pg.launches = e->last_launches - l0;
+    pg.recompute = e->last_recompute - r0;
+    W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
+    return W2D_OK;
+}
+
 int check_err(w2d_engine* e)
 {
     unsigned h = 0;
@@ -703,6 +767,8 @@ void w2d_engine_destroy(w2d_engine* e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->g_fwd.reset();
     e->g_bwd.reset();
+    e->g_model.reset();
+    e->g_bcorr.reset();
     for (DevBuf<float>* b : {&e->sponge_lut, &e->sponge_arr, &e->waves, &e->v2dt2, &e->staging,
                              &e->wavelet, &e->data, &e->rec_out, &e->snaps, &e->ckpt, &e->image,
                              &e->illum, &e->stack_img, &e->stack_ill})
@@ -759,6 +825,8 @@ int w2d_engine_set_graphs(w2d_engine* e, int on)
     e->use_graphs = on ? 1 : 0;
     e->g_fwd.reset();
     e->g_bwd.reset();
+    e->g_model.reset();
+    e->g_bcorr.reset();
     return W2D_OK;
 }
 
@@ -838,14 +906,21 @@ int w2d_forward(w2d_engine* e, int vel_slot, const float* wavelet, int nt, int s
     e->last_storage = 0;
     const float dt2inj = (float)(e->dt_d * e->dt_d);
     cudaEventRecord(e->ev0, e->stream);
-    if ((rc = forward_begin(e, dt2inj))) return rc;
-    FwdOpts o;
-    o.nt = nt;
-    o.interval = snapshot_interval;
-    o.n_rec = n_rec;
-    o.rec_out = n_rec > 0 ? e->rec_out.p : nullptr;
-    o.snaps = snaps_out ? e->snaps.p : nullptr;
-    if ((rc = run_forward_steps(e, vel_slot, o, 0, nt, 0.0, dt2inj))) return rc;
+    auto pass = [&]() -> int {
+        int r;
+        if ((r = forward_begin(e, dt2inj))) return r;
+        FwdOpts o;
+        o.nt = nt;
+        o.interval = snapshot_interval;
+        o.n_rec = n_rec;
+        o.rec_out = n_rec > 0 ? e->rec_out.p : nullptr;
+        o.snaps = snaps_out ? e->snaps.p : nullptr;
+        return run_forward_steps(e, vel_slot, o, 0, nt, 0.0, dt2inj);
+    };
+    const int kind = (vel_slot << 2) | (snaps_out ? 1 : 0) | (n_rec > 0 ? 2 : 0);
+    if ((rc = run_pass(e, e->g_model, pass_key(e, 2, nt, snapshot_interval, kind, 0, n_rec),
+                       pass)))
+        return rc;
     cudaEventRecord(e->ev1, e->stream);
     if (n_rec > 0)
         W2D_CUDA_TRY(cudaMemcpyAsync(rec_out, e->rec_out.p, (size_t)nt * n_rec * 4,
@@ -901,13 +976,19 @@ int w2d_backward_correlate(w2d_engine* e, int vel_slot, const float* data, int n
     const float dt2inj = (float)(e->dt_d * e->dt_d);
     const float img_dt = (float)(e->dt_d * (double)snapshot_interval);
     cudaEventRecord(e->ev0, e->stream);
-    if (n_rec > 0) {
-        if ((rc = backward_begin(e, nt, n_rec, dt2inj))) return rc;
-    } else {
-        if ((rc = zero_pass(e, 1))) return rc;
-    }
-    if ((rc = run_backward_steps(e, vel_slot, nt, snapshot_interval, n_rec, nt - 1, 0,
-                                 n_snaps > 0 ? e->snaps.p : nullptr, 0, n_snaps, img_dt, dt2inj)))
+    auto pass = [&]() -> int {
+        int r;
+        if (n_rec > 0) {
+            if ((r = backward_begin(e, nt, n_rec, dt2inj))) return r;
+        } else {
+            if ((r = zero_pass(e, 1))) return r;
+        }
+        return run_backward_steps(e, vel_slot, nt, snapshot_interval, n_rec, nt - 1, 0,
+                                  n_snaps > 0 ? e->snaps.p : nullptr, 0, n_snaps, img_dt,
+                                  dt2inj);
+    };
+    if ((rc = run_pass(e, e->g_bcorr,
+                       pass_key(e, 3, nt, snapshot_interval, vel_slot, n_snaps, n_rec), pass)))
         return rc;
     cudaEventRecord(e->ev1, e->stream);
     if ((rc = download_field(e, image, e->image.p))) return rc;
@@ -922,69 +1003,6 @@ namespace {
 
 // Forward + backward migration of one shot whose wavelet and data are already
 // on the device (e->cur_w, e->cur_data) and whose geometry is set.
-// Everything a pass's launches hold: when it matches a cached graph, replaying the
-// graph issues exactly the launches the host code would.
-std::vector<uintptr_t> pass_key(const w2d_engine* e, int pass, int nt, int interval, int mode,
-                                int seg, int n_rec)
-{
-    std::vector<uintptr_t> k = {
-        (uintptr_t)pass, (uintptr_t)nt, (uintptr_t)interval, (uintptr_t)mode, (uintptr_t)seg,
-        (uintptr_t)n_rec, (uintptr_t)e->tile.warps, (uintptr_t)e->tile.rpw, (uintptr_t)e->pdl,
-        (uintptr_t)e->l2_hints, (uintptr_t)e->use_lut, (uintptr_t)e->use_arr,
-        (uintptr_t)e->tm_tz, (uintptr_t)e->waves.p, (uintptr_t)e->snaps.p, (uintptr_t)e->ckpt.p,
-        (uintptr_t)e->v2dt2.p, (uintptr_t)e->image.p, (uintptr_t)e->illum.p,
-        (uintptr_t)e->cur_w, (uintptr_t)e->cur_data, (uintptr_t)e->rec_ptr.p,
-        (uintptr_t)e->rec_list.p, (uintptr_t)e->shot.p, (uintptr_t)e->err.p,
-        (uintptr_t)e->sponge_lut.p, (uintptr_t)e->sponge_arr.p};
-    for (int i = 0; i < 6; ++i) k.push_back((uintptr_t)e->perm[i]);
-    return k;
-}
-
-// Run one pass: replay its cached graph when the key matches, else capture the pass
-// from `body` (the host code that launches it), instantiate and launch the graph.  With
-// graphs off, or in a launch mode that keeps host-side state, `body` runs directly.  A
-// capture the runtime refuses turns graphs off for this engine and runs `body`.
-template <typename F>
-int run_pass(w2d_engine* e, w2d_engine::PassGraph& pg, std::vector<uintptr_t> key, F&& body)
-{
-    if (!e->use_graphs || e->two_step || e->persistent) return body();
-    if (pg.exec && pg.key == key) {
-        W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
-        e->last_launches += pg.launches;
-        e->last_recompute += pg.recompute;
-        return W2D_OK;
-    }
-    pg.reset();
-    const long long l0 = e->last_launches, r0 = e->last_recompute;
-    W2D_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = body();
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
-    if (rc || ce != cudaSuccess || !graph) {
-        // Nothing captured has run.  Whatever refused the capture (the pass's own
-        // launches are checked again below), run this and later passes as direct
-        // launches on this engine.
-        cudaGetLastError();
-        if (graph) cudaGraphDestroy(graph);
-        e->use_graphs = 0;
-        e->last_launches = l0;
-        e->last_recompute = r0;
-        return body();
-    }
-    const cudaError_t ie = cudaGraphInstantiate(&pg.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) {
-        pg.exec = nullptr;
-        set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
-        return W2D_ECUDA;
-    }
-    pg.key = std::move(key);
-    pg.launches = e->last_launches - l0;
-    pg.recompute = e->last_recompute - r0;
-    W2D_CUDA_TRY(cudaGraphLaunch(pg.exec, e->stream));
-    return W2D_OK;
-}
-
 int migrate_core(w2d_engine* e, int nt, int n_rec, int snapshot_interval, int storage,
                  float* image_out, float* illum_out)
 {
