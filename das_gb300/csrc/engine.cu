@@ -602,9 +602,13 @@ int run_pass(w2d_engine* e, w2d_engine::PassGraph& pg, std::vector<uintptr_t> ke
     const cudaError_t ie = cudaGraphInstantiate(&pg.exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ie != cudaSuccess) {
+        // as above: nothing has run; launch directly from now on
+        cudaGetLastError();
         pg.exec = nullptr;
-        set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
-        return W2D_ECUDA;
+        e->use_graphs = 0;
+        e->last_launches = l0;
+        e->last_recompute = r0;
+        return body();
     }
     pg.key = std::move(key);
     pg.launches = e->last_launches - l0;
