@@ -431,9 +431,12 @@ def run_ours(args, dist):
     eng_api.migrate_shot(fm_p, pin_w, shots[0], sv.src_iz, pin_g[0], sv.rec_ix, sv.rec_iz, interval)
     dist.barrier()
     t0 = time.perf_counter()
+    calls = []
     for k in range(ke):
+        tc = time.perf_counter()
         img, ill = eng_api.migrate_shot(fm_p, pin_w, shots[W + k], sv.src_iz, pin_g[k], sv.rec_ix,
                                         sv.rec_iz, interval)
+        calls.append(((time.perf_counter() - tc) * 1e3, solver.last_stats()["device_ms"]))
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = pts * ke * dist.world / e2e_s / 1e9
     h2d = gathers[0].nbytes + sv.wavelet.nbytes + 2 * sv.vel_mig.nbytes + rix.nbytes
@@ -480,6 +483,8 @@ def run_ours(args, dist):
                             "algorithmic_bytes_per_launch": per_launch},
                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h), "steps": ke,
+                       "per_call_ms": [round(c, 2) for c, _ in calls],
+                       "per_call_device_ms": [round(d, 2) for _, d in calls],
                        "api": "TSWRTMEngine.migrate_shot (pinned host arrays)"},
                "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                "wall_s_timed_region": wall, "accuracy": acc}
@@ -988,7 +993,7 @@ def main():
     ap.add_argument("--storage", default="auto", choices=["auto", "all", "checkpoint"])
     ap.add_argument("--tile", default="")
     ap.add_argument("--cpu-nt", type=int, default=1500)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--accuracy", type=int, default=1)
     ap.add_argument("--distinct-gathers", type=int, default=2)
     args = ap.parse_args()
