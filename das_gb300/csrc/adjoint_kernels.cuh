@@ -76,11 +76,18 @@ __global__ void __launch_bounds__(WARPS * 32)
         mbar_init(bar, 1);
         fence_mbar_init();
         mbar_expect_tx(bar, T::TX_BYTES);
-        tma_load_2d(ta1, &maps.a1, x0 - AC_HX, z0 - 2, bar);
+        // the model, the forward field P[n] (recomputed before this segment's adjoint steps)
+        // and a[n+2] (two launches back): issued before the dependency wait.  Each adjoint
+        // step releases its dependents only after its own wait, so when this one started the
+        // step before the previous one had completed.
         tma_load_2d(tb, &maps.c, x0 - AC_HX, z0 - 2, bar);
         tma_load_2d(tp, &maps.pf, x0 - AC_HX, z0 - 2, bar);
         tma_load_2d(ta2, &maps.a2, x0, z0, bar);
     }
+    // a[n+1] is the previous launch's output (and the gradient it updated): after the wait
+    grid_dep_wait();
+    grid_dep_launch();
+    if (threadIdx.x == 0) tma_load_2d(ta1, &maps.a1, x0 - AC_HX, z0 - 2, bar);
     __syncthreads();
     // a CTA-uniform decision: a partial exit before the warp shuffles would be undefined
     if (__syncthreads_or(!mbar_wait_bounded(bar, 0))) {
@@ -135,16 +142,18 @@ __global__ void __launch_bounds__(WARPS * 32)
     }
 }
 
+// pdl: a programmatic dependent of the stream's previous operation, which must then be
+// an adjoint step (it releases this launch only after its own wait).
 template <int WARPS, int RPW>
 inline cudaError_t launch_adjoint_step(const AdjMaps& m, const AcGeom& g, const AdjStep& s,
-                                       cudaStream_t st)
+                                       cudaStream_t st, int pdl = 0)
 {
     using T = AdjTile<WARPS, RPW>;
     const cudaError_t e = set_smem_once<acoustic_adjoint_kernel<WARPS, RPW>>((int)T::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     dim3 grid((g.nx + AC_TX - 1) / AC_TX, (g.nz + T::TZ - 1) / T::TZ);
-    acoustic_adjoint_kernel<WARPS, RPW><<<grid, WARPS * 32, T::SMEM_BYTES, st>>>(m, g, s);
-    return cudaGetLastError();
+    return launch_ex(acoustic_adjoint_kernel<WARPS, RPW>, grid, dim3(WARPS * 32), T::SMEM_BYTES,
+                     st, pdl, m, g, s);
 }
 
 }  // namespace w2d

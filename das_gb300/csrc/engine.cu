@@ -1601,6 +1601,7 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
                                      e->nz, e->ldx, AC_SW, hz)))
             return rc;
     const AcGeom g = geom(e);
+    bool adj_chain = false;  // the stream's last operation is an adjoint step
     auto adj = [&](int n, const CUtensorMap& pf) -> int {
         AdjMaps m;
         m.a1 = e->mcurr(3 + (n + 1) % 3);
@@ -1612,9 +1613,11 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
         s.grad = f->grad_c.p;
         s.resid_row = n >= 1 ? e->data.p + (size_t)(n - 1) * n_rec : nullptr;
         s.err = e->err.p;
-        cudaError_t ce = e->tile.warps == 4 ? launch_adjoint_step<4, 4>(m, g, s, e->stream)
-                                            : launch_adjoint_step<8, 4>(m, g, s, e->stream);
+        const int pdl = e->pdl && adj_chain;
+        cudaError_t ce = e->tile.warps == 4 ? launch_adjoint_step<4, 4>(m, g, s, e->stream, pdl)
+                                            : launch_adjoint_step<8, 4>(m, g, s, e->stream, pdl);
         W2D_CUDA_TRY(ce);
+        adj_chain = true;
         e->last_launches++;
         return W2D_OK;
     };
@@ -1639,6 +1642,7 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
             r.slot0 = a;
             if ((rc = run_forward_steps(e, 0, r, a, b, 0.0, dt2inj))) return rc;
             e->last_recompute += b - a;
+            adj_chain = false;  // the segment's first adjoint step waits for the stream
         }
         for (int n = b - 1; n >= a; --n)
             if ((rc = adj(n, f->seg_maps[n - a]))) return rc;
