@@ -349,6 +349,27 @@ __device__ __forceinline__ void ac_tile_body(const float* smem, const AcGeom& g,
     // stores, boundary rows, receivers and next-step injection
     const int src_ix = g.shot[0], src_iz = g.shot[1], rec_iz = g.shot[2];
     const bool rec_active = (s.rec_out != nullptr) || (s.inj_data != nullptr);
+    // The receiver row's table lookups for this lane's four columns, as three rounds of
+    // independent loads (CSR bounds, first receiver index, its data sample) rather than
+    // one dependent chain per column: the first receiver of column ixb+j is rk[j] (-1:
+    // none), further ones (rare) are read in the loop below.
+    int kb[4] = {0, 0, 0, 0}, ke[4] = {0, 0, 0, 0}, rk[4] = {-1, -1, -1, -1};
+    float rd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const bool warp_rec = rec_active && col_ok && rec_iz >= zr0 && rec_iz < zr0 + RPW &&
+                          rec_iz < nz;
+    if (warp_rec) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool in = ixb + j < nx;
+            kb[j] = in ? __ldg(g.rec_ptr + ixb + j) : 0;
+            ke[j] = in ? __ldg(g.rec_ptr + ixb + j + 1) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) rk[j] = ke[j] > kb[j] ? __ldg(g.rec_list + kb[j]) : -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            rd[j] = (s.inj_data && rk[j] >= 0) ? __ldg(s.inj_data + rk[j]) : 0.0f;
+    }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
         const int iz = zr0 + r;
@@ -387,12 +408,17 @@ __device__ __forceinline__ void ac_tile_body(const float* smem, const AcGeom& g,
             const bool at_rec = rec_active && iz == rec_iz;
             const bool at_src = s.inj_w && iz == src_iz && ix == src_ix;
             if (!wr && (at_rec || at_src)) val = row_next[ix];
-            if (at_rec) {
-                const int k0 = __ldg(g.rec_ptr + ix), k1 = __ldg(g.rec_ptr + ix + 1);
-                if (s.rec_out)
-                    for (int k = k0; k < k1; ++k) s.rec_out[__ldg(g.rec_list + k)] = val;
-                if (s.inj_data && k1 > k0) {
-                    for (int k = k0; k < k1; ++k)
+            if (at_rec && rk[j] >= 0) {
+                // receivers of the column in index order (the reference's per-receiver
+                // loop): sampling sees the value before any injection
+                const int k0 = kb[j], k1 = ke[j];
+                if (s.rec_out) {
+                    s.rec_out[rk[j]] = val;
+                    for (int k = k0 + 1; k < k1; ++k) s.rec_out[__ldg(g.rec_list + k)] = val;
+                }
+                if (s.inj_data) {
+                    val = fadd(val, fmul(rd[j], s.dt2_inj));
+                    for (int k = k0 + 1; k < k1; ++k)
                         val = fadd(val, fmul(__ldg(s.inj_data + __ldg(g.rec_list + k)), s.dt2_inj));
                     wr = true;
                 }
