@@ -803,6 +803,8 @@ def run_served(args, dist):
              "busy_s_by_kind": kind_s}
     served_first = [x.latency for x in out[:m]]
     plain["makespan_s"] = plain_span
+    plain["achieved_gpts_per_s"] = sum(j.counted_points for r in trace[:m]
+                                       for j in r.shots) / plain_span / 1e9
     out_line = {"metric": "served RTM shots/s", "value": st["shots_per_s"], "unit": "shots/s",
                 "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": f"Poisson trace of {len(trace)} jobs at {args.serve_rate} "

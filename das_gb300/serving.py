@@ -179,13 +179,20 @@ class RTMServer:
         out = [responses[r.job_id] for r in trace]
         lat = [r.latency for r in out]
         span_jobs = trace[-1].arrival - trace[0].arrival if len(trace) > 1 else 0.0
+        # counted points (2 nz nx nt per shot) of every request, acoustic and elastic
+        total_pts = float(sum(sh.counted_points for r in trace for sh in r.shots))
         stats = {"jobs": len(out), "shots": sum(len(r.shots) for r in trace),
                  "makespan_s": makespan, "p50_latency_s": percentile(lat, 50),
                  "p99_latency_s": percentile(lat, 99),
                  "shots_per_s": sum(len(r.shots) for r in trace) / makespan if makespan else 0.0,
+                 # acoustic points advanced by the batch engine's replays
                  "gpts_per_s": pts / makespan / 1e9 if makespan else 0.0,
                  "device_busy_frac": busy_ms / 1e3 / makespan if makespan else 0.0,
                  "offered_jobs_per_s": (len(trace) - 1) / span_jobs if span_jobs > 0 else None,
+                 # offered load (all requests' points over the arrival span) against the
+                 # load served (the same points over the makespan)
+                 "offered_gpts_per_s": total_pts / span_jobs / 1e9 if span_jobs > 0 else None,
+                 "achieved_gpts_per_s": total_pts / makespan / 1e9 if makespan else 0.0,
                  "max_active_shots": max_active}
         for kind in sorted({r.kind for r in out}):
             lk = [r.latency for r in out if r.kind == kind]
