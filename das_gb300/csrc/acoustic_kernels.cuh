@@ -46,10 +46,23 @@ struct AcGeom {
     const float* sponge_lut;  // n_sponge+1 values by integer frame distance (LUT mode)
     const int* rec_ptr;       // CSR over columns: receivers of column ix are
     const int* rec_list;      //   rec_list[rec_ptr[ix] .. rec_ptr[ix+1])
-    const int* shot;          // device ints {src_ix, src_iz, rec_iz}
+    const int* shot;          // device ints {src_ix, src_iz, rec_iz, n_rec, rec_c0}: rec_c0
+                              //   is the column of receiver 0 when receiver r sits at
+                              //   column rec_c0 + r for every r, else -1
     int l2_hints;             // 1: keep p_curr, vel^2 dt^2 and p_next in L2 (evict-last),
                               //    stream p_prev (evict-first)
 };
+
+// rec_c0 of the shot ints: the column of receiver 0 when receiver r sits at column
+// rec_c0 + r for every r (then each column holds at most one receiver and its index
+// follows from the column), else -1.
+inline int receivers_consecutive_c0(const int* rec_ix, int n_rec)
+{
+    if (n_rec <= 0) return -1;
+    for (int r = 1; r < n_rec; ++r)
+        if (rec_ix[r] != rec_ix[0] + r) return -1;
+    return rec_ix[0];
+}
 
 // Per-launch pointers (all optional ones may be null).
 struct AcStep {
@@ -349,23 +362,34 @@ __device__ __forceinline__ void ac_tile_body(const float* smem, const AcGeom& g,
     // stores, boundary rows, receivers and next-step injection
     const int src_ix = g.shot[0], src_iz = g.shot[1], rec_iz = g.shot[2];
     const bool rec_active = (s.rec_out != nullptr) || (s.inj_data != nullptr);
-    // The receiver row's table lookups for this lane's four columns, as three rounds of
-    // independent loads (CSR bounds, first receiver index, its data sample) rather than
-    // one dependent chain per column: the first receiver of column ixb+j is rk[j] (-1:
-    // none), further ones (rare) are read in the loop below.
+    // The receiver row's lookups for this lane's four columns.  Receivers on consecutive
+    // columns in index order (rec_c0 >= 0, the usual surface line): receiver ix - rec_c0,
+    // one round of loads (the data samples).  Otherwise three rounds of independent loads
+    // (CSR bounds, first receiver index, its data sample) rather than one dependent chain
+    // per column.  The first receiver of column ixb+j is rk[j] (-1: none); further ones
+    // (CSR only, rare) are read in the loop below.
     int kb[4] = {0, 0, 0, 0}, ke[4] = {0, 0, 0, 0}, rk[4] = {-1, -1, -1, -1};
     float rd[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const bool warp_rec = rec_active && col_ok && rec_iz >= zr0 && rec_iz < zr0 + RPW &&
                           rec_iz < nz;
     if (warp_rec) {
+        const int rec_c0 = g.shot[4], n_rec = g.shot[3];
+        if (rec_c0 >= 0) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const bool in = ixb + j < nx;
-            kb[j] = in ? __ldg(g.rec_ptr + ixb + j) : 0;
-            ke[j] = in ? __ldg(g.rec_ptr + ixb + j + 1) : 0;
+            for (int j = 0; j < 4; ++j) {
+                const int r = ixb + j - rec_c0;
+                rk[j] = (ixb + j < nx && r >= 0 && r < n_rec) ? r : -1;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const bool in = ixb + j < nx;
+                kb[j] = in ? __ldg(g.rec_ptr + ixb + j) : 0;
+                ke[j] = in ? __ldg(g.rec_ptr + ixb + j + 1) : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) rk[j] = ke[j] > kb[j] ? __ldg(g.rec_list + kb[j]) : -1;
         }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) rk[j] = ke[j] > kb[j] ? __ldg(g.rec_list + kb[j]) : -1;
 #pragma unroll
         for (int j = 0; j < 4; ++j)
             rd[j] = (s.inj_data && rk[j] >= 0) ? __ldg(s.inj_data + rk[j]) : 0.0f;

@@ -601,6 +601,7 @@ int submit_job(w2d_batch* b, const w2d_shot_desc* d, int mode, int* slot_out)
     h.shot_ints[1] = d->src_iz;
     h.shot_ints[2] = d->rec_iz;
     h.shot_ints[3] = n_rec;
+    h.shot_ints[4] = receivers_consecutive_c0(d->rec_ix, n_rec);
     h.nt = nt;
     h.interval = interval;
     h.n_rec = n_rec;

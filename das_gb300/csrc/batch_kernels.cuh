@@ -32,7 +32,7 @@ namespace w2d {
 // Device-resident descriptor of one shot of a batch.
 struct BShot {
     AcGeom g;           // g.shot points at shot_ints of this descriptor
-    int shot_ints[4];   // src_ix, src_iz, rec_iz, n_rec
+    int shot_ints[5];   // src_ix, src_iz, rec_iz, n_rec, rec_c0 (AcGeom::shot)
     int nt, interval, n_rec;
     int tiles_x, tiles_z, ntiles;
     int k_end;          // 2 * nt phase steps

@@ -397,9 +397,9 @@ int set_shot(w2d_engine* e, int src_ix, int src_iz, const int* rec_ix, int n_rec
     for (int r = 0; r < n_rec; ++r) list[fill[rec_ix[r]]++] = r;
     int rc;
     if ((rc = e->rec_ptr.ensure(e->nx + 1)) || (rc = e->rec_list.ensure(list.size())) ||
-        (rc = e->shot.ensure(4)))
+        (rc = e->shot.ensure(5)))
         return rc;
-    int sh[4] = {src_ix, src_iz, rec_iz, n_rec};
+    int sh[5] = {src_ix, src_iz, rec_iz, n_rec, receivers_consecutive_c0(rec_ix, n_rec)};
     e->h_shot[0] = src_ix;
     e->h_shot[1] = src_iz;
     e->h_shot[2] = rec_iz;
@@ -749,10 +749,10 @@ int w2d_engine_create(w2d_engine** out, int nx, int nz, float dx, float dz, doub
             e->use_arr = true;
         }
     }
-    if ((rc = e->shot.ensure(4)) || (rc = e->rec_ptr.ensure(nx + 1)) ||
+    if ((rc = e->shot.ensure(5)) || (rc = e->rec_ptr.ensure(nx + 1)) ||
         (rc = e->rec_list.ensure(1)))
         return fail(rc);
-    int sh[4] = {-1, -1, -1, 0};
+    int sh[5] = {-1, -1, -1, 0, -1};
     cudaMemcpy(e->shot.p, sh, sizeof sh, cudaMemcpyHostToDevice);
     cudaMemset(e->rec_ptr.p, 0, (nx + 1) * 4);
     if ((rc = ensure_tensor_maps(e))) return fail(rc);

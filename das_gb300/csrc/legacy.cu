@@ -26,7 +26,7 @@ struct LegacyCtx {
     size_t dev_cap = 0;    // floats
     float* pin = nullptr;  // page-locked staging (packed nz x nx planes)
     size_t pin_cap = 0;    // floats
-    int* shot = nullptr;   // {-1,-1,-1,0}: no source, no receivers
+    int* shot = nullptr;   // {-1,-1,-1,0,-1}: no source, no receivers
     int* rec_ptr = nullptr;
     int rec_cap = 0;
     unsigned* err = nullptr;
@@ -40,9 +40,9 @@ int prepare(int n_planes_dev, size_t plane_dev, int n_planes_pin, size_t plane_p
 {
     if (!g.st) W2D_CUDA_TRY(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
     if (!g.shot) {
-        W2D_CUDA_TRY(cudaMalloc(&g.shot, 4 * sizeof(int)));
+        W2D_CUDA_TRY(cudaMalloc(&g.shot, 5 * sizeof(int)));
         W2D_CUDA_TRY(cudaMalloc(&g.err, sizeof(unsigned)));
-        const int sh[4] = {-1, -1, -1, 0};
+        const int sh[5] = {-1, -1, -1, 0, -1};
         W2D_CUDA_TRY(cudaMemcpyAsync(g.shot, sh, sizeof sh, cudaMemcpyHostToDevice, g.st));
         W2D_CUDA_TRY(cudaMemsetAsync(g.err, 0, sizeof(unsigned), g.st));
         W2D_CUDA_TRY(cudaStreamSynchronize(g.st));

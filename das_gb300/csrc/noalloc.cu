@@ -60,7 +60,7 @@ constexpr size_t kOffVel = 3 * kPlaneMax;               // 1 plane
 constexpr size_t kOffLut = 4 * kPlaneMax;               // kSpongeMax + 1 floats
 constexpr size_t kOffPtr = kOffLut + kSpongeMax + 64;   // kNxMax + 1 ints
 constexpr size_t kOffList = kOffPtr + kNxMax + 64;      // kRecMax ints
-constexpr size_t kOffShot = kOffList + kRecMax + 64;    // 4 ints
+constexpr size_t kOffShot = kOffList + kRecMax + 64;    // 5 ints
 constexpr size_t kOffErr = kOffShot + 64;               // 1 unsigned
 constexpr size_t kWords = kOffErr + 64;
 static_assert(kWords * 4 <= W2D_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the array");
@@ -146,7 +146,7 @@ int w2d_forward_noalloc(const float* vel_dev, const float* wavelet_dev, int nt, 
     const int n_lut = n_sponge > 0 ? n_sponge : 0;
     g_lut[0] = 1.0f;
     for (int d = 1; d <= n_lut; ++d) g_lut[d] = cerjan_value(d, sponge_alpha);
-    const int sh[4] = {src_ix, src_iz, rec_iz, n_rec};
+    const int sh[5] = {src_ix, src_iz, rec_iz, n_rec, receivers_consecutive_c0(rec_ix, n_rec)};
 
     // tensor maps are host-side encodings of the scratch planes: build them before any
     // work is queued, so that a failure here leaves nothing running
