@@ -76,6 +76,7 @@ _SIGS = {
                                 c_int, c_void_p]),
     "w2d_fwi_gradient": (c_int, [c_void_p, c_void_p, c_void_p]),
     "w2d_fwi_set_segment": (c_int, [c_void_p, c_int]),
+    "w2d_fwi_set_adjoint_form": (c_int, [c_void_p, c_int]),
     "w2d_flood_models": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, ctypes.c_double,
                                  ctypes.c_double, c_void_p, c_void_p, c_void_p, c_void_p]),
     "w2d_engine_synchronize": (c_int, [c_void_p]),

@@ -113,6 +113,7 @@ struct w2d_engine {
     int l2_hints = 0;
     int persistent = 0, pdl = 1;  // step launch mode (measured fastest: one CTA per tile + PDL)
     int fwi_seg = 0;  // differentiable path: steps per checkpoint segment (0: sqrt(3 nt))
+    int adj_cells = 0;  // differentiable path: the per-cell adjoint kernel instead of the vectorised one
     bool chain = false;  // the last operation on the stream is a step kernel launched by step()
     bool last_step1 = false;  // ... and it was the one-step kernel (one CTA per tile)
     DevBuf<unsigned> tile_counter;
@@ -1576,6 +1577,13 @@ int w2d_fwi_set_segment(w2d_engine* e, int steps)
     return W2D_OK;
 }
 
+int w2d_fwi_set_adjoint_form(w2d_engine* e, int cells)
+{
+    W2D_CHECK_ARG(e, "engine is NULL");
+    e->adj_cells = cells ? 1 : 0;
+    return W2D_OK;
+}
+
 int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
 {
     W2D_ON_DEVICE_OF(e);
@@ -1614,8 +1622,9 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev)
         s.resid_row = n >= 1 ? e->data.p + (size_t)(n - 1) * n_rec : nullptr;
         s.err = e->err.p;
         const int pdl = e->pdl && adj_chain;
-        cudaError_t ce = e->tile.warps == 4 ? launch_adjoint_step<4, 4>(m, g, s, e->stream, pdl)
-                                            : launch_adjoint_step<8, 4>(m, g, s, e->stream, pdl);
+        cudaError_t ce = e->tile.warps == 4
+                             ? launch_adjoint_step<4, 4>(m, g, s, e->stream, pdl, e->adj_cells)
+                             : launch_adjoint_step<8, 4>(m, g, s, e->stream, pdl, e->adj_cells);
         W2D_CUDA_TRY(ce);
         adj_chain = true;
         e->last_launches++;

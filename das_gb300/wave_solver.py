@@ -142,6 +142,13 @@ class WaveSolver2D:
         The gradient is the same bit for bit either way."""
         _lib.check(self._lib.w2d_fwi_set_segment(self._eng(), int(steps)))
 
+    def set_adjoint_form(self, form: str = "tiled") -> None:
+        """Adjoint kernel of the differentiable path: "tiled" (vectorised, the default) or
+        "cells" (the per-cell kernel it is checked against; the same to rounding)."""
+        if form not in ("tiled", "cells"):
+            raise ValueError("adjoint form must be 'tiled' or 'cells'")
+        _lib.check(self._lib.w2d_fwi_set_adjoint_form(self._eng(), 1 if form == "cells" else 0))
+
     def close(self):
         if getattr(self, "_engine", None) is not None:
             self._lib.w2d_engine_destroy(self._engine)

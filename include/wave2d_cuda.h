@@ -216,6 +216,10 @@ int w2d_fwi_gradient(w2d_engine* e, const float* resid_dev, float* grad_dev);
  * nt or more keeps every forward state of the run (no recomputation, nt planes
  * of device memory).  The gradient is the same bit for bit either way. */
 int w2d_fwi_set_segment(w2d_engine* e, int steps);
+/* Form of the adjoint kernel of w2d_fwi_gradient: 0 (the default) the vectorised
+ * kernel, 1 the per-cell kernel it is checked against.  The two agree to float32
+ * rounding (they differ only in the compiler's contraction choices). */
+int w2d_fwi_set_adjoint_form(w2d_engine* e, int cells);
 int w2d_engine_synchronize(w2d_engine* e);
 
 /* ---- Elastic modelling and gradient (no reference counterpart: the reference only

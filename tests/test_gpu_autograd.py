@@ -83,6 +83,45 @@ def test_gradient_relates_to_rtm_image():
     assert c < -0.8  # d2/dt2 ~ -omega^2: anti-correlated with the zero-lag image
 
 
+@pytest.mark.parametrize("nz,nx,fs,layout", [
+    (50, 100, True, "line"),       # one partial tile column, receivers on row 3
+    (70, 300, True, "gaps"),       # receivers every third column (the CSR lookup)
+    (90, 520, False, "line"),      # no free surface: the sponge on all four sides
+    (130, 700, True, "shuffled"),  # receivers in no column order, some columns twice
+])
+def test_vectorised_adjoint_equals_per_cell_adjoint(nz, nx, fs, layout):
+    """The vectorised adjoint kernel (float4 lanes, register window, plain tiles stored
+    as float4) against the per-cell kernel on grids with frame tiles, partial tiles,
+    the receiver row, the free-surface fold and the sponge: the same gradient to float32
+    rounding (they differ only in the compiler's contraction choices)."""
+    from das_gb300.autograd import misfit_and_gradient
+    from das_gb300.wave_solver import WaveSolver2D, ricker_wavelet
+    rng = np.random.default_rng(nz + nx)
+    z = np.arange(nz)[:, None]
+    v = (1800.0 + 12.0 * z + 40.0 * rng.standard_normal((nz, nx))).astype(np.float32)
+    w, _ = ricker_wavelet(15.0, DT, 0.2)
+    if layout == "line":
+        rix = np.arange(2, nx - 2)
+    elif layout == "gaps":
+        rix = np.arange(2, nx - 2, 3)
+    else:
+        rix = rng.permutation(np.concatenate([np.arange(2, nx - 2, 2), np.arange(5, 60, 7)]))
+    riz = 2 if fs else 3
+    d_obs = (1e-9 * rng.standard_normal((len(w), len(rix)))).astype(np.float32)
+    s = WaveSolver2D(nx, nz, DX, DX, DT, n_sponge=12, free_surface_top=fs)
+    grads = {}
+    for form in ("cells", "tiled"):
+        s.set_adjoint_form(form)
+        J, g = misfit_and_gradient(s, v, w, nx // 3, 6, rix, riz, d_obs)
+        grads[form] = g
+    s.close()
+    a, b = grads["tiled"].astype(np.float64), grads["cells"].astype(np.float64)
+    assert np.abs(b).max() > 0
+    rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+    print(f"{nz} x {nx} ({layout}, free surface {fs}): vectorised vs per-cell rel L2 {rel:.2e}")
+    assert rel < 1e-5
+
+
 def test_gradient_of_8000_steps_on_the_large_grid():
     """An 8000-step shot on the 1000 x 4000 grid.  By default the forward states come
     back from checkpoints (about sqrt(3 nt) steps per segment, one segment of states
