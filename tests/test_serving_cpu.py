@@ -180,3 +180,18 @@ def test_a_shot_larger_than_the_arena_is_refused():
     eng = FakeEngine(capacity=10, slots=2)
     with pytest.raises(MemoryError):
         RTMServer(eng).serve(trace, realtime=False)
+
+
+def test_elastic_batches_split_by_grid_length_receivers_and_budget(monkeypatch):
+    """ElasticExecutor groups consecutive shots that share grid, length and receivers,
+    each group no larger than the per-worker budget allows (here three shots)."""
+    from das_gb300.elastic import ElasticExecutor
+    ex = object.__new__(ElasticExecutor)  # the grouping only: no worker threads
+    monkeypatch.setattr(ElasticExecutor, "_cap", lambda self, shot: 3)
+    a = [_shot(40, 80, 100, t) for t in range(5)]        # same grid and length
+    b = [_shot(40, 80, 120, t) for t in range(5, 7)]     # another length
+    c = [_shot(50, 80, 120, t) for t in range(7, 8)]     # another grid
+    d = _shot(50, 80, 120, 8)
+    d.receiver_ix = np.arange(0, 80, 2)                  # other receivers
+    groups = ex._batches(a + b + c + [d])
+    assert [[s.tag for s in g] for g in groups] == [[0, 1, 2], [3, 4], [5, 6], [7], [8]]
