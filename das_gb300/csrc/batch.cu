@@ -16,6 +16,7 @@
 #include <map>
 #include <vector>
 
+#include "arena.h"
 #include "batch_kernels.cuh"
 #include "small_kernels.cuh"
 #include "w2d_common.cuh"
@@ -63,7 +64,7 @@ struct w2d_batch {
     cudaStream_t st_up = nullptr;  // shot admission (uploads, set-up kernels)
     char* arena = nullptr;
     size_t arena_bytes = 0;
-    std::map<size_t, size_t> free_blocks;  // offset -> bytes
+    ArenaFreeList free_list{kAlign};  // the arena's free blocks
     int max_shots = 0;
     BShot* d_shots = nullptr;
     BMaps* d_maps = nullptr;
@@ -99,46 +100,11 @@ struct w2d_batch {
 
 namespace {
 
-bool arena_alloc(w2d_batch* b, size_t bytes, size_t* off)
-{
-    bytes = (bytes + kAlign - 1) / kAlign * kAlign;
-    for (auto it = b->free_blocks.begin(); it != b->free_blocks.end(); ++it) {
-        if (it->second >= bytes) {
-            *off = it->first;
-            const size_t rest = it->second - bytes;
-            const size_t noff = it->first + bytes;
-            b->free_blocks.erase(it);
-            if (rest) b->free_blocks[noff] = rest;
-            return true;
-        }
-    }
-    return false;
-}
+bool arena_alloc(w2d_batch* b, size_t bytes, size_t* off) { return b->free_list.alloc(bytes, off); }
 
-void arena_free(w2d_batch* b, size_t off, size_t bytes)
-{
-    bytes = (bytes + kAlign - 1) / kAlign * kAlign;
-    auto it = b->free_blocks.emplace(off, bytes).first;
-    auto nx = std::next(it);
-    if (nx != b->free_blocks.end() && it->first + it->second == nx->first) {
-        it->second += nx->second;
-        b->free_blocks.erase(nx);
-    }
-    if (it != b->free_blocks.begin()) {
-        auto pv = std::prev(it);
-        if (pv->first + pv->second == it->first) {
-            pv->second += it->second;
-            b->free_blocks.erase(it);
-        }
-    }
-}
+void arena_free(w2d_batch* b, size_t off, size_t bytes) { b->free_list.free(off, bytes); }
 
-size_t largest_free(const w2d_batch* b)
-{
-    size_t m = 0;
-    for (auto& kv : b->free_blocks) m = std::max(m, kv.second);
-    return m;
-}
+size_t largest_free(const w2d_batch* b) { return b->free_list.largest(); }
 
 template <int W, int R>
 cudaError_t set_attr_and_occ(int* grid)
@@ -337,7 +303,7 @@ int w2d_batch_create(w2d_batch** out, unsigned long long arena_bytes, int max_sh
         return fail(W2D_ENOMEM);
     }
     b->arena_bytes = arena_bytes;
-    b->free_blocks[0] = (size_t)arena_bytes / kAlign * kAlign;
+    b->free_list.reset((size_t)arena_bytes);
     if (cudaMalloc(&b->d_shots, sizeof(BShot) * max_shots) != cudaSuccess ||
         cudaMalloc(&b->d_maps, sizeof(BMaps) * max_shots) != cudaSuccess ||
         cudaMalloc(&b->d_active, sizeof(int) * max_shots) != cudaSuccess ||
