@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 
 // Vectorised form (the default): each lane owns four consecutive x points (float4
 // shared-memory reads, x neighbours by warp shuffles, a five-row register window
-// along z for c * a[n+1] and for P[n]), float4 stores of a[n] and of the gradient on
+// along z for c * a[n+1], formed as its rows are read, and for P[n]), float4 stores of a[n] and of the gradient on
 // tiles away from the frame; tiles touching the frame, the receiver row or the
 // sponge apply the per-point rules of the per-cell form to the same values.
 template <int WARPS, int RPW>
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(WARPS * 32)
     using T = AdjTile<WARPS, RPW>;
     extern __shared__ __align__(128) float smem[];
     float* ta1 = smem;
-    float* tb = smem + T::H_FLOATS;  // c, then c * a[n+1]
+    float* tb = smem + T::H_FLOATS;  // c
     float* tp = smem + 2 * T::H_FLOATS;
     float* ta2 = smem + 3 * T::H_FLOATS;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + T::FLOATS);
@@ -183,18 +183,6 @@ __global__ void __launch_bounds__(WARPS * 32)
         if (threadIdx.x == 0) atomicOr(s.err, ERR_TMA_TIMEOUT);
         return;
     }
-    // c * a[n+1] over the halo box, in place of c
-    for (int i = threadIdx.x; i < T::H_FLOATS / 4; i += blockDim.x) {
-        float4 c = reinterpret_cast<const float4*>(tb)[i];
-        const float4 a = reinterpret_cast<const float4*>(ta1)[i];
-        c.x = c.x * a.x;
-        c.y = c.y * a.y;
-        c.z = c.z * a.z;
-        c.w = c.w * a.w;
-        reinterpret_cast<float4*>(tb)[i] = c;
-    }
-    __syncthreads();
-
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nx = g.nx, nz = g.nz, ldx = g.ldx;
     const int ixb = x0 + 4 * lane;
@@ -205,18 +193,25 @@ __global__ void __launch_bounds__(WARPS * 32)
     auto ld4 = [&](const float* box, int row) {
         return *reinterpret_cast<const float4*>(&box[row * AC_SW + sc]);
     };
-    auto x_halo = [&](const float* box, const float4& w, int row, float e[8]) {
+    // c * a[n+1] of a box row (the product is formed where it is read: no extra pass)
+    auto ldb = [&](int row) {
+        const float4 c = ld4(tb, row), a = ld4(ta1, row);
+        return make_float4(c.x * a.x, c.y * a.y, c.z * a.z, c.w * a.w);
+    };
+    // box value at a shared-memory index: P[n], or c * a[n+1] when prod
+    auto at = [&](const float* box, bool prod, int i) { return prod ? tb[i] * ta1[i] : box[i]; };
+    auto x_halo = [&](const float* box, bool prod, const float4& w, int row, float e[8]) {
         float l2 = __shfl_up_sync(0xffffffffu, w.z, 1);
         float l1 = __shfl_up_sync(0xffffffffu, w.w, 1);
         float r1 = __shfl_down_sync(0xffffffffu, w.x, 1);
         float r2 = __shfl_down_sync(0xffffffffu, w.y, 1);
         if (lane == 0) {
-            l2 = box[row * AC_SW + AC_HX - 2];
-            l1 = box[row * AC_SW + AC_HX - 1];
+            l2 = at(box, prod, row * AC_SW + AC_HX - 2);
+            l1 = at(box, prod, row * AC_SW + AC_HX - 1);
         }
         if (lane == 31) {
-            r1 = box[row * AC_SW + AC_HX + AC_TX];
-            r2 = box[row * AC_SW + AC_HX + AC_TX + 1];
+            r1 = at(box, prod, row * AC_SW + AC_HX + AC_TX);
+            r2 = at(box, prod, row * AC_SW + AC_HX + AC_TX + 1);
         }
         e[0] = l2;
         e[1] = l1;
@@ -246,17 +241,17 @@ __global__ void __launch_bounds__(WARPS * 32)
                 (g.free_surface || z0 >= n);
     }
 
-    float4 b0 = ld4(tb, sr0), b1 = ld4(tb, sr0 + 1), b2 = ld4(tb, sr0 + 2), b3 = ld4(tb, sr0 + 3);
+    float4 b0 = ldb(sr0), b1 = ldb(sr0 + 1), b2 = ldb(sr0 + 2), b3 = ldb(sr0 + 3);
     float4 q0 = ld4(tp, sr0), q1 = ld4(tp, sr0 + 1), q2 = ld4(tp, sr0 + 2), q3 = ld4(tp, sr0 + 3);
     float lam_row1[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
         const int iz = zr0 + r;
         const int srow = sr0 + r + 2;
-        const float4 b4 = ld4(tb, srow + 2), q4 = ld4(tp, srow + 2);
+        const float4 b4 = ldb(srow + 2), q4 = ld4(tp, srow + 2);
         float eb[8], eq[8];
-        x_halo(tb, b2, srow, eb);
-        x_halo(tp, q2, srow, eq);
+        x_halo(tb, true, b2, srow, eb);
+        x_halo(tp, false, q2, srow, eq);
         const float4 a1 = ld4(ta1, srow);
         const float4 a2 = *reinterpret_cast<const float4*>(&ta2[(sr0 + r) * AC_TX + 4 * lane]);
         float lam[4], gr[4];
