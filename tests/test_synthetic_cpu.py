@@ -67,3 +67,52 @@ def test_large_configuration_and_seed():
     other = plain_large(seed=1, nt=8000)
     assert other.meta["faults"] != faults
     assert int(np.argmax(sv.wavelet)) == round(1.0 / 6.0 / 2.5e-4)
+
+
+def test_batched_gathers_configuration():
+    """256 uneven gathers: nx in [400, 2000], nz in [200, 600], dx 5 m, nt in [1500, 4000],
+    3-5 Hz Ricker, smoothed layered models with 1-3 faults within vp 1500-3500 m/s; dt
+    0.5 ms keeps the CFL number at or below 0.5."""
+    from das_gb300.synthetic import batched_gathers
+    gs = batched_gathers(256, seed=0)
+    assert len(gs) == 256
+    for g in gs:
+        assert 400 <= g.nx <= 2000 and 200 <= g.nz <= 600 and 1500 <= g.nt <= 4000
+        assert g.dx == 5.0 and g.dt == 5e-4 and 3.0 <= g.f0 <= 5.0
+        assert g.vel.shape == (g.nz, g.nx) and g.vel.dtype == np.float32
+        assert g.vel.min() >= 1500.0 and g.vel.max() <= 3500.0
+        assert 40 <= g.src_ix < g.nx - 40
+        cfl = float(g.vel.max()) * g.dt * np.sqrt(2.0) / g.dx
+        assert cfl <= 0.5
+    # uneven, and reproducible from the seed
+    assert len({(g.nz, g.nx, g.nt) for g in gs}) > 200
+    again = batched_gathers(256, seed=0)
+    assert all(np.array_equal(a.vel, b.vel) for a, b in zip(gs[:8], again[:8]))
+
+
+def test_elastic_fault_zone_configuration():
+    """1024 x 2048, dx 2 m: vs 300 -> 1200 m/s with depth, a 20 m low-velocity zone dipping
+    70 degrees; vp = 1.73 vs and density from Gardner's relation (rho = 310 vp^0.25)."""
+    torch = pytest.importorskip("torch")
+    from das_gb300.elastic import gardner_parameters
+    from das_gb300.synthetic import elastic_fault_zone
+    vs = elastic_fault_zone()
+    assert vs.shape == (1024, 2048) and vs.dtype == np.float32
+    assert vs[0, 0] == pytest.approx(300.0) and vs[-1, 0] == pytest.approx(1200.0)
+    z = np.arange(1024) * 2.0
+    background = 300.0 + 900.0 * z / z[-1]
+    slow = vs < background[:, None] - 1e-3
+    # the zone: 70 % of the background, about 20 m wide across the dip
+    assert np.allclose(vs[slow], 0.7 * np.broadcast_to(background[:, None], vs.shape)[slow],
+                       rtol=1e-6)
+    widths = slow.sum(axis=1) * 2.0 * np.sin(np.deg2rad(70.0))
+    assert np.all((widths[:900] > 14.0) & (widths[:900] < 26.0))
+    # it dips 70 degrees: its centre moves by dz / tan(70) to the right per metre of depth
+    cols = [np.mean(np.nonzero(slow[iz])[0]) for iz in (100, 500, 900)]
+    slope = (cols[2] - cols[0]) * 2.0 / (z[900] - z[100])
+    assert slope == pytest.approx(1.0 / np.tan(np.deg2rad(70.0)), rel=0.02)
+    lam, mu, bx, bz = gardner_parameters(torch.tensor(vs[:4, :4].astype(np.float64)))[:4]
+    vp = 1.73 * vs[:4, :4].astype(np.float64)
+    rho = 310.0 * vp ** 0.25
+    np.testing.assert_allclose(mu.numpy(), rho * vs[:4, :4] ** 2, rtol=1e-6)
+    np.testing.assert_allclose(lam.numpy(), rho * vp * vp - 2.0 * rho * vs[:4, :4] ** 2, rtol=1e-6)
