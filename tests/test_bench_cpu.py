@@ -50,3 +50,31 @@ def test_roofline_inputs_of_the_default_line():
     assert bench.bytes_per_shot(Survey, 2) == 2 * 8000 * P * 16 + 4000 * P * 12 * 2
     # per counted point (2 nz nx nt per shot): 22 B, as the batch line assumes
     assert bench.bytes_per_shot(Survey, 2) / (2 * P * 8000) == 22.0
+
+
+def test_served_trace_follows_its_configuration():
+    """The served trace: Poisson arrivals at 20 jobs/s; grid sides log-uniform from
+    128 x 256 to 1024 x 4096; nt in [1000, 8000]; 1-32 shots per job sharing the job's
+    model; about 80 % acoustic and 20 % elastic jobs; reproducible from the seed."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    tr = bench._served_trace(40, 20.0, 0)
+    assert len(tr) == 40
+    arr = np.array([r.arrival for r in tr])
+    assert np.all(np.diff(arr) >= 0)
+    rate = (len(tr) - 1) / (arr[-1] - arr[0])
+    assert 10.0 < rate < 40.0  # 20 jobs/s, 39 exponential gaps
+    kinds = [r.kind for r in tr]
+    assert 0.1 <= kinds.count("elastic") / len(tr) <= 0.35
+    for r in tr:
+        s0 = r.shots[0]
+        assert 1 <= len(r.shots) <= 32
+        assert 128 <= s0.nz <= 1024 and 256 <= s0.nx <= 4096
+        assert 1000 <= len(s0.wavelet) <= 8000
+        assert all((s.nz, s.nx, len(s.wavelet)) == (s0.nz, s0.nx, len(s0.wavelet))
+                   for s in r.shots)
+        assert all(s.vel_fwd is s0.vel_fwd for s in r.shots)  # one model per job
+    again = bench._served_trace(40, 20.0, 0)
+    assert [(r.kind, r.shots[0].nz, r.shots[0].nx, len(r.shots)) for r in again] == \
+        [(r.kind, r.shots[0].nz, r.shots[0].nx, len(r.shots)) for r in tr]
